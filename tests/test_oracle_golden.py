@@ -1,0 +1,206 @@
+"""Pin the CPU oracle against golden vectors written by the reference itself (CPU only)."""
+
+import math
+
+import numpy as np
+import pytest
+
+import problems as P
+from oracle import rk_oracle as O
+
+ETD35_NAMES = ("a21", "a31", "a32", "a41", "a43", "a51", "a52", "a54", "a61", "a62", "a63", "a65",
+               "a71", "a73", "a74", "a75", "a76")
+
+
+def _close(a, b, rtol):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    scale = max(np.max(np.abs(b)), 1e-300)
+    return np.max(np.abs(a - b)) <= rtol * scale
+
+
+@pytest.mark.parametrize("tag", ["ks", "nls"])
+@pytest.mark.parametrize("h", [0.05, 0.3])
+def test_diag_coeffs_match_reference(golden, tag, h):
+    g = golden("coeffs")
+    lin = g[f"coef_{tag}_lin"]
+    ht = f"{tag}_h{h}"
+    c = O.diag_coeffs("ETD35", lin, h)
+    for name, key in (("E14", "EL14"), ("E12", "EL12"), ("E34", "EL34"), ("E", "EL")):
+        assert np.array_equal(c[name], g[f"coef_ETD35_{ht}_{key}"])
+    for name in ETD35_NAMES:
+        assert _close(c[name], g[f"coef_ETD35_{ht}_{name}"], 1e-15), name
+    c = O.diag_coeffs("ETD5", lin, h)
+    for name, key in (("a71", "b1"), ("a73", "b3"), ("a74", "b4"), ("a75", "b5"), ("a76", "b6"), ("a61", "a61")):
+        assert _close(c[name], g[f"coef_ETD5_{ht}_{key}"], 1e-15), name
+    for meth in ("ETD34", "ETD4"):
+        c = O.diag_coeffs(meth, lin, h)
+        keys = {"a51": "b1", "a52": "b2", "a54": "b4"} if meth == "ETD4" else {}
+        assert np.array_equal(c["E"], g[f"coef_{meth}_{ht}_EL"])
+        assert np.array_equal(c["E2"], g[f"coef_{meth}_{ht}_EL2"])
+        for name in ("a21", "a31", "a32", "a41", "a43", "a51", "a52", "a54"):
+            assert _close(c[name], g[f"coef_{meth}_{ht}_{keys.get(name, name)}"], 1e-15), (meth, name)
+    c = O.diag_coeffs("IF34", lin, h)
+    assert np.array_equal(c["E"], g[f"coef_IF34_{ht}_EL"])
+    assert np.array_equal(c["E2"], g[f"coef_IF34_{ht}_EL2"])
+    c = O.diag_coeffs("IF45DP", lin, h)
+    for name in ("E15", "E310", "E45", "E89", "E"):
+        assert np.array_equal(c[name], g[f"coef_IF45DP_{ht}_EL{name[1:]}"])
+    for name in ("a21", "a31", "a32", "a41", "a42", "a43", "a51", "a52", "a53", "a54", "a61", "a62", "a63",
+                 "a64", "a65", "a71", "a73", "a74", "a75", "r1", "r3", "r4", "r5"):
+        assert _close(c[name], g[f"coef_IF45DP_{ht}_{name}"], 1e-15), name
+    np.testing.assert_array_equal([c["a76"], c["r6"], c["r7"]], g[f"coef_IF45DP_{ht}_scalars"])
+
+
+def test_diag_coeffs_nondefault_etdconfig(golden):
+    g = golden("coeffs")
+    cfg = O.ETDConfig(modecutoff=0.5, contour_points=16, contour_radius=2.0)
+    c = O.diag_coeffs("ETD35", g["coef_ks_lin"], 0.1, cfg)
+    for name in ("a21", "a54", "a61", "a71", "a75", "a76"):
+        assert _close(c[name], g[f"coef_ETD35cfg2_{name}"], 1e-15), name
+
+
+@pytest.mark.parametrize("method", ["ETD4", "ETD5", "IF4"])
+def test_fixed_step_kdv(golden, method):
+    g = golden("fixed_step")
+    kx, lin, nl, u0 = P.kdv_problem()
+    np.testing.assert_array_equal(u0, g["kdv_u0"])
+    s = O.OracleSolver(method, lin, nl)
+    uf = s.evolve(u0, 0.0, 0.025 * 200, 0.025, store_data=False)
+    assert _close(uf, g[f"kdv_{method}_final"], 1e-13)
+    s = O.OracleSolver(method, lin, nl)
+    s.evolve(u0, 0.0, 0.5, 0.025, store_data=True, store_freq=4)
+    np.testing.assert_allclose(s.t, g[f"kdv_{method}_snap_t"], rtol=0, atol=1e-15)
+    assert _close(np.array(s.u), g[f"kdv_{method}_snap_u"], 1e-14)
+
+
+@pytest.mark.parametrize("method", ["ETD4", "IF4", "ETD5"])
+def test_fixed_step_ks(golden, method):
+    g = golden("fixed_step")
+    x, kx, lin, nl = P.ks(128, 32 * np.pi)
+    u0 = g["ks128_u0"]
+    s = O.OracleSolver(method, lin, nl)
+    uf = s.evolve(u0, 0.0, 10.0, 0.02, store_data=False)
+    assert _close(uf, g[f"ks128_{method}_final"], 1e-12)
+
+
+def test_adaptive_ks_config1_if34(golden):
+    g = golden("adaptive")
+    kx, lin, nl, u0 = P.ks_config1()
+    s = O.OracleSolver("IF34", lin, nl, O.SolverConfig())
+    uf = s.evolve(u0, 0.0, 50.0, store_freq=20)
+    ref_s = g["ks1024_IF34_s"]
+    got_s = np.array([r[2] for r in s.log])
+    assert got_s.shape == ref_s.shape
+    np.testing.assert_allclose(got_s, ref_s, rtol=1e-9)
+    np.testing.assert_allclose(s.t, g["ks1024_IF34_t"], rtol=1e-13)
+    assert _close(uf, g["ks1024_IF34_final"], 1e-9)
+    assert _close(s.u[5], g["ks1024_IF34_u5"], 1e-11)
+
+
+@pytest.mark.parametrize("method", ["ETD35", "ETD34", "IF34", "IF45DP"])
+def test_adaptive_ks256(golden, method):
+    g = golden("adaptive")
+    kx, lin, nl, u0 = P.ks256_problem(golden)
+    s = O.OracleSolver(method, lin, nl, O.SolverConfig(epsilon=1e-5))
+    uf = s.evolve(u0, 0.0, 0.5 if method == "IF45DP" else 20.0, store_freq=10)
+    got_s = np.array([r[2] for r in s.log])
+    np.testing.assert_allclose(got_s, g[f"ks256_{method}_s"], rtol=1e-9)
+    np.testing.assert_allclose(s.t, g[f"ks256_{method}_t"], rtol=1e-13)
+    assert _close(uf, g[f"ks256_{method}_final"], 1e-9)
+
+
+def test_adaptive_nls256_etd35(golden):
+    g = golden("adaptive")
+    kx, lin, nl = P.nls256()
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-6))
+    uf = s.evolve(g["nls256_u0"], 0.0, 2.0, store_freq=5)
+    np.testing.assert_allclose([r[2] for r in s.log], g["nls256_ETD35_s"], rtol=1e-9)
+    np.testing.assert_allclose(s.t, g["nls256_ETD35_t"], rtol=1e-13)
+    assert _close(uf, g["nls256_ETD35_final"], 1e-11)
+
+
+def test_adaptive_burgers_etd35(golden):
+    g = golden("adaptive")
+    x, kx, lin, nl = P.burgers(512, 0.02)
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-5))
+    uf = s.evolve(g["burg512_u0"], 0.0, 5.0, store_data=False)
+    np.testing.assert_allclose([r[2] for r in s.log], g["burg512_ETD35_s"], rtol=1e-9)
+    assert _close(uf, g["burg512_ETD35_final"], 1e-11)
+
+
+@pytest.mark.parametrize("method", ["ETD34", "ETD35", "IF34"])
+def test_adaptive_kdv(golden, method):
+    g = golden("adaptive")
+    kx, lin, nl, u0 = P.kdv_problem()
+    s = O.OracleSolver(method, lin, nl, O.SolverConfig(epsilon=1e-4))
+    uf = s.evolve(u0, 0.0, 5.0, h_init=0.025, store_data=False)
+    assert _close(uf, g[f"kdv_{method}_adapt_final"], 1e-11)
+
+
+def test_step_api_kdv_etd35(golden):
+    g = golden("adaptive")
+    kx, lin, nl, u0 = P.kdv_problem()
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-1))
+    uu = u0.copy()
+    for _ in range(200):
+        uu, hh, hs = s.step(uu, 0.025)
+        assert hh == 0.025
+    assert _close(uu, g["kdv_ETD35_step200"], 1e-13)
+
+
+def test_controller_clamps(golden):
+    g = golden("controller")
+    cfg = O.SolverConfig()
+    for s, rej, acc in zip(g["ctl_s"], g["ctl_reject"], g["ctl_accept"]):
+        assert O.reject_step_size(float(s), 0.1, cfg) == rej
+        if math.isfinite(s):
+            assert O.accept_step_size(float(s), 0.1, cfg) == acc
+
+
+def test_controller_compute_s(golden):
+    g = golden("controller")
+    cfg = O.SolverConfig()
+    for u, e, s in zip(g["ctl_u"], g["ctl_e"], g["ctl_s_out"]):
+        assert O.compute_s(u, e, cfg, 4) == pytest.approx(s, rel=1e-15)
+
+
+def test_failures(golden):
+    g = golden("failure")
+    assert int(g["fail_explosive"]) == 2
+    s = O.OracleSolver("ETD35", np.array([-1.0]), lambda u: 1e12 * u, O.SolverConfig(epsilon=1e-6))
+    with pytest.raises(O.MinimumStepReached):
+        s.evolve(np.array([1.0]), 0, 1e-3, h_init=1e-2, store_data=False)
+    assert int(g["fail_burg"]) == 2
+    x, kx, lin, nl = P.burgers(512, float(g["fail_burg_nu"]))
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-5))
+    with pytest.raises(O.MinimumStepReached):
+        s.evolve(g["fail_burg_u0"], 0.0, 5.0, store_data=False)
+
+
+def test_dense_allen_cahn(golden):
+    g = golden("dense")
+    x, D = P.cheb(20)
+    np.testing.assert_allclose(D, g["cheb20_D"], rtol=0, atol=1e-12)
+    x, lin, nl = P.allen_cahn(20)
+    np.testing.assert_allclose(lin, g["ac20_lin"], rtol=0, atol=1e-12)
+    w0 = g["ac20_w0"]
+    cfg = O.ETDConfig(contour_points=32, contour_radius=10)
+    C = O.dense_coeffs("ETD35", g["ac20_lin"], 0.05, cfg)
+    for name in ("a21", "a54", "a65", "a76"):
+        assert _close(C[name], g[f"ac20_ETD35_dense_{name}"], 1e-12), name
+    assert _close(C["E"], g["ac20_ETD35_dense_EL"], 1e-13)
+    s = O.OracleSolver("ETD35", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), cfg)
+    assert _close(s.evolve(w0, 0, 60, store_data=False), g["ac20_ETD35_nondiag_final"], 1e-9)
+    s = O.OracleSolver("ETD35", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), diagonalize=True)
+    assert _close(s.evolve(w0, 0, 60, store_data=False), g["ac20_ETD35_diagz_final"], 1e-9)
+    s = O.OracleSolver("ETD34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), diagonalize=True)
+    assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_ETD34_diagz_final"], 1e-9)
+    s = O.OracleSolver("IF34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), diagonalize=True)
+    assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_IF34_diagz_final"], 1e-9)
+    s = O.OracleSolver("IF34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4))
+    assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_IF34_dense_final"], 1e-9)
+    s = O.OracleSolver("IF4", g["ac20_lin"], nl)
+    assert _close(s.evolve(w0, 0, 2, 0.01, store_data=False), g["ac20_IF4_dense_final"], 1e-12)
+    s = O.OracleSolver("ETD4", g["ac20_lin"], nl, etd_config=cfg)
+    assert _close(s.evolve(w0, 0, 2, 0.01, store_data=False), g["ac20_ETD4_dense_final"], 1e-12)
