@@ -1,0 +1,171 @@
+/*
+ * rkstiff_gb300 -- C ABI of the GB300 (sm_103a) stepping kernels.
+ *
+ * The reference (whalenpt/rkstiff) is pure Python and has no FFI; its boundary is the
+ * solver-object API.  This header is what a binding of that API binds: every entry
+ * point below replaces one reference routine, cited as file:line within the rkstiff
+ * project.  Plain C types only; every pointer marked [device] is a CUDA device pointer
+ * on the current device; `stream` is a cudaStream_t passed as void*.
+ *
+ * Return convention: 0 on success, a negative RK_E* code on an API/CUDA error
+ * (rk_last_error() gives the message).  Per-instance outcomes of a run are written to
+ * rk_inst_state.status (RK_ST_*), never returned.
+ */
+#ifndef RKSTIFF_GB300_H
+#define RKSTIFF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RK_ABI_VERSION 1
+
+/* twiddle table length: supports complex FFTs and real grids up to this many points */
+#define RK_TW_N 8192
+
+/* methods: the seven solver classes of the reference */
+enum {
+  RK_IF34 = 0,   /* rkstiff/if34.py:260   (adaptive, q=4, FSAL)                 */
+  RK_ETD35 = 1,  /* rkstiff/etd35.py:723  (adaptive, q=4, N1 recomputed)        */
+  RK_ETD34 = 2,  /* rkstiff/etd34.py:439  (adaptive, q=4, FSAL)                 */
+  RK_IF45DP = 3, /* rkstiff/if45dp.py:8   (adaptive, q=5, FSAL, diagonal only)  */
+  RK_ETD4 = 4,   /* rkstiff/etd4.py:311   (constant step)                       */
+  RK_ETD5 = 5,   /* rkstiff/etd5.py       (constant step)                       */
+  RK_IF4 = 6     /* rkstiff/if4.py:202    (constant step)                       */
+};
+
+enum { RK_FP64 = 0, RK_FP32 = 1 };
+
+/* built-in fused nonlinearities (the nl_func closures of rkstiff/models.py and README) */
+enum {
+  RK_NL_NONE = 0, /* N(u) = 0 (pure linear problem)                                     */
+  RK_NL_UUX = 1,  /* N(u) = c rfft(irfft(u) * irfft(i kx u)) on a real grid:
+                     KS (README.md:94-97, c=-1), Burgers (models.py:189-192, c=-1),
+                     KdV (models.py:140-143, c=-6)                                    */
+  RK_NL_NLS = 2   /* N(u) = fft(i c |v|^2 v), v = ifft(u), on a complex grid (c=1)    */
+};
+
+enum { RK_RUN_EVOLVE = 0, RK_RUN_STEP = 1 };
+
+/* per-instance outcome codes */
+enum {
+  RK_ST_RUNNING = -1, /* not started / resumable                                      */
+  RK_ST_DONE = 0,     /* reached tf                                                   */
+  RK_ST_MAX_LOOPS = 1,/* more than 50 retries in one step (solveras.py:399-406)        */
+  RK_ST_MIN_STEP = 2, /* h < minh after a reject (solveras.py:407-410)                 */
+  RK_ST_ITER_CAP = 4, /* the launch's accepted-step bound was hit (resumable)          */
+  RK_ST_SNAP_FULL = 5,/* the snapshot buffer filled (resumable)                        */
+  RK_ST_STEP_DONE = 6 /* RK_RUN_STEP: one accepted step was taken                      */
+};
+
+/* error codes */
+enum {
+  RK_OK = 0,
+  RK_E_ARG = -1,
+  RK_E_CUDA = -2,
+  RK_E_UNSUPPORTED = -3,
+  RK_E_SIZE = -4
+};
+
+/* adaptive controller settings: SolverConfig, rkstiff/solveras.py:27-169 */
+typedef struct rk_controller {
+  double epsilon, incr_f, decr_f, safety_f, adapt_cutoff, minh;
+} rk_controller;
+
+/* psi-function settings: ETDConfig, rkstiff/etd.py:46-131 */
+typedef struct rk_etd_config {
+  double modecutoff;
+  double contour_radius;
+  int32_t contour_points;
+  int32_t reserved;
+} rk_etd_config;
+
+/* per-instance controller state (the attributes rkstiff keeps on the solver object:
+ * __tc/__tf and _accept of solveras.py:281-282, _h_coeff of etd.py:226) plus counters */
+typedef struct rk_inst_state {
+  double t;          /* current time                                               */
+  double tf;         /* final time                                                 */
+  double h;          /* step size of the next attempt                              */
+  double h_coeff;    /* step size the cached coefficients were built for (NaN: none)*/
+  double h_used;     /* step size of the last accepted step                        */
+  double h_suggest;  /* suggestion after the last accepted step                    */
+  double s_last;     /* controller factor s of the last attempt                    */
+  double reserved_d;
+  int32_t status;    /* RK_ST_*                                                    */
+  int32_t accept;    /* last attempt accepted (reference _accept)                  */
+  int32_t snap_count;/* snapshots written in the current launch                     */
+  int32_t reserved_i;
+  int64_t steps, attempts, rejects, nl_evals, coeff_updates, reserved_l;
+} rk_inst_state;
+
+/* One batched run over independent diagonal-operator instances.
+ * Modes of instance i live at [mode_off[i], mode_off[i] + m_i) of lin_op / kx / u,
+ * m_i = n_i/2 + 1 for RK_NL_UUX (real grid), n_i otherwise. */
+typedef struct rk_batch {
+  int32_t method;        /* RK_IF34 ... RK_IF4                                        */
+  int32_t precision;     /* RK_FP64 / RK_FP32                                         */
+  int32_t coef_complex;  /* 0: the operator is real, coefficients stored real         */
+  int32_t nl_kind;       /* RK_NL_*                                                   */
+  double nl_coef;        /* constant c of the nonlinearity                            */
+  int64_t n_inst;
+  int32_t n_max;           /* largest n over the instances (sizes the FFT buffers)    */
+  int32_t reserved0;
+  const int32_t* n;        /* [device] grid points per instance (power of two)       */
+  const int64_t* mode_off; /* [device] first mode of each instance                   */
+  const int32_t* order;    /* [device] processing order (NULL: 0..n_inst-1)           */
+  const double* lin_op;    /* [device] complex128 interleaved operator per mode       */
+  const double* kx;        /* [device] wavenumber per mode (RK_NL_UUX)               */
+  void* u;                 /* [device] complex64/complex128 state, in/out             */
+  rk_inst_state* state;    /* [device] per-instance state, in/out                     */
+  void* slab;              /* [device] scratch: coefficient, stage and work arrays    */
+  const int64_t* slab_off; /* [device] byte offset of each instance's scratch         */
+  const void* twiddle;     /* [device] RK_TW_N twiddles exp(-2 pi i k/RK_TW_N), in T  */
+  int32_t* queue;          /* [device] one int32 work counter, zeroed by rk_evolve    */
+  int32_t store_freq;      /* snapshot every store_freq accepted steps; 0 = never     */
+  int32_t snap_cap;        /* snapshots per instance per launch                       */
+  void* snap_u;            /* [device] snap_cap*m_i states per instance at snap_cap*mode_off */
+  double* snap_t;          /* [device] snap_cap times per instance                     */
+  int64_t max_steps;       /* accepted steps per instance per launch (safety bound)    */
+  int32_t run_mode;        /* RK_RUN_EVOLVE / RK_RUN_STEP                              */
+  int32_t threads;         /* threads per instance group, a multiple of 32 <= 256 (0: 256) */
+  rk_controller ctl;
+  rk_etd_config etd;
+} rk_batch;
+
+/* ABI version and last error message (thread-local). */
+int rk_abi_version(void);
+const char* rk_last_error(void);
+
+/* Fill twiddle tables exp(-2 pi i k/RK_TW_N), k < RK_TW_N, in FP64 (tw64, complex128)
+ * and rounded to FP32 (tw32, complex64).  Either pointer may be NULL. [device] */
+int rk_fill_twiddles(void* tw64, void* tw32, void* stream);
+
+/* Bytes of per-instance scratch rk_evolve needs for an instance with m modes.
+ * Replaces the coefficient / stage arrays the reference allocates per solver object
+ * (e.g. rkstiff/etd35.py:129-155). */
+int64_t rk_slab_bytes(int32_t method, int32_t precision, int32_t coef_complex, int64_t m);
+
+/* Coefficient arrays of `method` at step h for a diagonal operator, FP64 math stored in
+ * `precision`: the diagonal update_coeffs routines rkstiff/etd35.py:169-288,
+ * etd34.py:96-149, etd4.py:87-139, etd5.py:115-203, if34.py:81-93, if4.py:72-83,
+ * if45dp.py:183-238.  lin_op: m complex128 [device]; out: rk_num_coeffs(method) arrays of
+ * m entries each (real or complex T per coef_complex), array c at out + c*m. */
+int rk_num_coeffs(int32_t method);
+int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m, const double* lin_op,
+              double h, const rk_etd_config* etd, void* out, void* stream);
+
+/* Run (or resume) the adaptive or constant-step evolve loop of every instance on the
+ * device: BaseSolverAS.evolve/step (rkstiff/solveras.py:336-650) with _compute_s,
+ * _reject_step_size and _accept_step_size, or BaseSolverCS.evolve/step
+ * (rkstiff/solvercs.py:163-279), each attempt running the method's stage program
+ * (_update_stages) with the built-in nonlinearity fused between in-shared-memory FFTs. */
+int rk_evolve(const rk_batch* b, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RKSTIFF_GB300_H */

@@ -1,0 +1,82 @@
+"""Execution backend of the solver classes: the fused device path for a diagonal
+operator with a built-in nonlinearity."""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .engine import DiagEnsemble, snapshot_views
+from .models import BuiltinNL
+
+
+def _to_output(t: torch.Tensor, like):
+    if isinstance(like, torch.Tensor):
+        return t.clone()
+    return t.detach().cpu().numpy().copy()
+
+
+class DiagBackend:
+    """One-instance ensemble kept alive across calls, so the coefficient cache and the
+    controller state (accept flag, h of the cached coefficients) persist like the
+    attributes of a reference solver object."""
+
+    def __init__(self, solver, method: str):
+        nl = solver.nl_func
+        if not isinstance(nl, BuiltinNL):
+            raise NotImplementedError(
+                "nl_func must be a built-in nonlinearity from rkstiff_gb300.models (fused device kernel); "
+                "arbitrary callables are not supported on this path")
+        opts = solver.device_options
+        self.solver = solver
+        self.ens = DiagEnsemble(method, [solver.lin_op], nl.kind, nl.coef, None if nl.kx is None else [nl.kx],
+                                [nl.n], precision=opts.precision, config=getattr(solver, "config", None),
+                                etd_config=getattr(solver, "etd_config", None), device=opts.device,
+                                threads=opts.threads)
+        self.snap_cap = max(1, int(opts.snap_cap))
+        self.reset()
+
+    def reset(self):
+        self.st = self.ens.fresh_state(0.0, np.inf, 0.0)
+
+    def _sync_config(self):
+        self.ens.set_config(getattr(self.solver, "config", None), getattr(self.solver, "etd_config", None))
+
+    def evolve(self, u, t0, tf, h, store_data, store_freq):
+        """Device evolve; appends snapshots to solver.t / solver.u; returns (u_final, status)."""
+        self._sync_config()
+        s = self.solver
+        u_dev = self.ens.pack_u([u])
+
+        def on_snaps(st, snap_u, snap_t):
+            ts, us = snapshot_views(self.ens, st, snap_u, snap_t, 0)
+            for tt, uu in zip(ts, us):
+                s.t.append(float(tt))
+                s.u.append(_to_output(uu, u))
+
+        freq = int(store_freq) if store_data else 0
+        if store_data and freq <= 0:
+            raise ValueError("store_freq must be a positive integer")
+        st = self.ens.evolve(u_dev, t0, tf, h, store_freq=freq, snap_cap=self.snap_cap, on_snapshots=on_snaps)
+        self.st = st
+        return _to_output(u_dev, u), int(st["status"][0])
+
+    def step(self, u, h):
+        self._sync_config()
+        u_dev = self.ens.pack_u([u])
+        st = self.st
+        st["t"] = 0.0
+        st["tf"] = np.inf
+        st["h"] = h
+        st["status"] = nat.RK_ST_RUNNING
+        st["snap_count"] = 0
+        self.ens.put_state(st)
+        self.ens.launch(u_dev, nat.RK_RUN_STEP)
+        self.st = self.ens.get_state()
+        return _to_output(u_dev, u), int(self.st["status"][0])
+
+    @property
+    def counters(self):
+        st = self.st
+        return {k: int(st[k][0]) for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates")}

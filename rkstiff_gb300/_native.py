@@ -1,0 +1,109 @@
+"""ctypes binding of librkstiff_gb300 (the C ABI declared in include/rkstiff_gb300.h).
+
+The library is required: importing the solver path without it raises, there is no
+CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+# enums (include/rkstiff_gb300.h)
+RK_IF34, RK_ETD35, RK_ETD34, RK_IF45DP, RK_ETD4, RK_ETD5, RK_IF4 = range(7)
+METHOD_IDS = {"IF34": RK_IF34, "ETD35": RK_ETD35, "ETD34": RK_ETD34, "IF45DP": RK_IF45DP,
+              "ETD4": RK_ETD4, "ETD5": RK_ETD5, "IF4": RK_IF4}
+RK_FP64, RK_FP32 = 0, 1
+RK_NL_NONE, RK_NL_UUX, RK_NL_NLS = 0, 1, 2
+RK_RUN_EVOLVE, RK_RUN_STEP = 0, 1
+RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
+RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE = 4, 5, 6
+RK_TW_N = 8192
+
+# number of stage arrays and coefficient arrays per method (mirrors rk_evolve.cuh Traits)
+STAGE_ARRAYS = {RK_ETD35: 6, RK_ETD5: 6, RK_ETD34: 5, RK_ETD4: 4, RK_IF34: 5, RK_IF4: 4, RK_IF45DP: 7}
+
+
+class RkController(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("epsilon", "incr_f", "decr_f", "safety_f", "adapt_cutoff", "minh")]
+
+
+class RkEtdConfig(ctypes.Structure):
+    _fields_ = [("modecutoff", ctypes.c_double), ("contour_radius", ctypes.c_double),
+                ("contour_points", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class RkBatch(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32), ("precision", ctypes.c_int32), ("coef_complex", ctypes.c_int32),
+        ("nl_kind", ctypes.c_int32), ("nl_coef", ctypes.c_double), ("n_inst", ctypes.c_int64),
+        ("n_max", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("n", ctypes.c_void_p), ("mode_off", ctypes.c_void_p), ("order", ctypes.c_void_p),
+        ("lin_op", ctypes.c_void_p), ("kx", ctypes.c_void_p), ("u", ctypes.c_void_p), ("state", ctypes.c_void_p),
+        ("slab", ctypes.c_void_p), ("slab_off", ctypes.c_void_p), ("twiddle", ctypes.c_void_p),
+        ("queue", ctypes.c_void_p), ("store_freq", ctypes.c_int32), ("snap_cap", ctypes.c_int32),
+        ("snap_u", ctypes.c_void_p), ("snap_t", ctypes.c_void_p), ("max_steps", ctypes.c_int64),
+        ("run_mode", ctypes.c_int32), ("threads", ctypes.c_int32),
+        ("ctl", RkController), ("etd", RkEtdConfig),
+    ]
+
+
+# rk_inst_state as a NumPy record (128 bytes)
+STATE_DTYPE = np.dtype([
+    ("t", "f8"), ("tf", "f8"), ("h", "f8"), ("h_coeff", "f8"), ("h_used", "f8"), ("h_suggest", "f8"),
+    ("s_last", "f8"), ("reserved_d", "f8"), ("status", "i4"), ("accept", "i4"), ("snap_count", "i4"),
+    ("reserved_i", "i4"), ("steps", "i8"), ("attempts", "i8"), ("rejects", "i8"), ("nl_evals", "i8"),
+    ("coeff_updates", "i8"), ("reserved_l", "i8"),
+])
+assert STATE_DTYPE.itemsize == 128
+
+# every symbol the header declares
+EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
+           "rk_evolve")
+
+_lib = None
+_lock = threading.Lock()
+
+
+class NativeError(RuntimeError):
+    """A C entry point returned an error code."""
+
+
+def load(build: bool = True) -> ctypes.CDLL:
+    """Load (building first if needed) the shared library and declare its signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.build() if build else _build.lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"rkstiff_gb300 native library missing at {path}; run rkstiff_gb300._build.build()")
+        lib = ctypes.CDLL(path)
+        vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+        lib.rk_abi_version.restype = ctypes.c_int
+        lib.rk_last_error.restype = ctypes.c_char_p
+        lib.rk_fill_twiddles.argtypes = [vp, vp, vp]
+        lib.rk_fill_twiddles.restype = ctypes.c_int
+        lib.rk_slab_bytes.argtypes = [i32, i32, i32, i64]
+        lib.rk_slab_bytes.restype = i64
+        lib.rk_num_coeffs.argtypes = [i32]
+        lib.rk_num_coeffs.restype = ctypes.c_int
+        lib.rk_coeffs.argtypes = [i32, i32, i32, i64, vp, dbl, ctypes.POINTER(RkEtdConfig), vp, vp]
+        lib.rk_coeffs.restype = ctypes.c_int
+        lib.rk_evolve.argtypes = [ctypes.POINTER(RkBatch), vp]
+        lib.rk_evolve.restype = ctypes.c_int
+        if lib.rk_abi_version() != 1:
+            raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
+        _lib = lib
+        return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = _lib.rk_last_error().decode() if _lib is not None else ""
+        raise NativeError(f"{what} failed ({rc}): {msg}")

@@ -1,0 +1,147 @@
+// C entry points of librkstiff_gb300 (declared in include/rkstiff_gb300.h).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <string>
+
+#include "rk_coeffs.cuh"
+#include "rk_evolve.cuh"
+#include "rk_launch.h"
+
+namespace rk {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return RK_OK;
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return RK_E_CUDA;
+}
+
+__global__ void twiddle_kernel(cx<double>* tw64, cx<float>* tw32) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= RK_TW_N) return;
+  double s, c;
+  // exp(-2 pi i k / N) = cos(pi * 2k/N) - i sin(pi * 2k/N)
+  sincospi(2.0 * (double)k / (double)RK_TW_N, &s, &c);
+  if (tw64) tw64[k] = cx<double>{c, -s};
+  if (tw32) tw32[k] = cx<float>{(float)c, (float)(-s)};
+}
+
+static int check_method(int method) {
+  if (method < RK_IF34 || method > RK_IF4) {
+    set_error("unknown method id " + std::to_string(method));
+    return RK_E_ARG;
+  }
+  return RK_OK;
+}
+
+}  // namespace rk
+
+using namespace rk;
+
+extern "C" {
+
+int rk_abi_version(void) { return RK_ABI_VERSION; }
+
+const char* rk_last_error(void) { return g_err.c_str(); }
+
+int rk_fill_twiddles(void* tw64, void* tw32, void* stream) {
+  twiddle_kernel<<<(RK_TW_N + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<cx<double>*>(tw64), reinterpret_cast<cx<float>*>(tw32));
+  return cuda_check(cudaGetLastError(), "twiddle launch");
+}
+
+int64_t rk_slab_bytes(int32_t method, int32_t precision, int32_t coef_complex, int64_t m) {
+  if (check_method(method) || m <= 0) return -1;
+  return slab_bytes(method, precision, coef_complex, m);
+}
+
+int rk_num_coeffs(int32_t method) {
+  if (check_method(method)) return RK_E_ARG;
+  return num_coeffs(method);
+}
+
+int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m, const double* lin_op, double h,
+              const rk_etd_config* etd, void* out, void* stream) {
+  if (int e = check_method(method)) return e;
+  if (m <= 0 || !lin_op || !out || !etd || (precision != RK_FP64 && precision != RK_FP32)) {
+    set_error("rk_coeffs: invalid argument");
+    return RK_E_ARG;
+  }
+  if (etd->contour_points < 2) {
+    set_error("rk_coeffs: contour_points must be > 1");
+    return RK_E_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (method) {
+    case RK_IF34: return launch_coeffs_IF34(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_ETD35: return launch_coeffs_ETD35(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_ETD34: return launch_coeffs_ETD34(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_IF45DP: return launch_coeffs_IF45DP(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_ETD4: return launch_coeffs_ETD4(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_ETD5: return launch_coeffs_ETD5(precision, coef_complex, m, lin_op, h, *etd, out, s);
+    case RK_IF4: return launch_coeffs_IF4(precision, coef_complex, m, lin_op, h, *etd, out, s);
+  }
+  return RK_E_ARG;
+}
+
+int rk_evolve(const rk_batch* b, void* stream) {
+  if (!b) {
+    set_error("rk_evolve: null batch");
+    return RK_E_ARG;
+  }
+  if (int e = check_method(b->method)) return e;
+  if (b->precision != RK_FP64 && b->precision != RK_FP32) {
+    set_error("rk_evolve: precision must be RK_FP64 or RK_FP32");
+    return RK_E_ARG;
+  }
+  if (b->nl_kind < RK_NL_NONE || b->nl_kind > RK_NL_NLS) {
+    set_error("rk_evolve: unknown nonlinearity kind");
+    return RK_E_ARG;
+  }
+  if (b->n_inst <= 0) return RK_OK;
+  if (!b->n || !b->mode_off || !b->lin_op || !b->u || !b->state || !b->slab || !b->slab_off || !b->twiddle ||
+      !b->queue) {
+    set_error("rk_evolve: null device pointer");
+    return RK_E_ARG;
+  }
+  if (b->nl_kind == RK_NL_UUX && !b->kx) {
+    set_error("rk_evolve: RK_NL_UUX needs kx");
+    return RK_E_ARG;
+  }
+  const int nmax = b->n_max;
+  const int limit = b->precision == RK_FP64 ? 4096 : 8192;
+  if (nmax < 4 || (nmax & (nmax - 1)) || nmax > limit) {
+    set_error("rk_evolve: n_max must be a power of two in [4, " + std::to_string(limit) + "]");
+    return RK_E_SIZE;
+  }
+  if (b->store_freq > 0 && (b->snap_cap <= 0 || !b->snap_u || !b->snap_t)) {
+    set_error("rk_evolve: snapshots requested without a snapshot buffer");
+    return RK_E_ARG;
+  }
+  if (b->etd.contour_points < 2) {
+    set_error("rk_evolve: contour_points must be > 1");
+    return RK_E_ARG;
+  }
+  const int thr = b->threads > 0 ? b->threads : 256;
+  if (thr % 32 || thr > 256) {
+    set_error("rk_evolve: threads must be a multiple of 32 and <= 256");
+    return RK_E_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (b->method) {
+    case RK_IF34: return launch_evolve_IF34(*b, s);
+    case RK_ETD35: return launch_evolve_ETD35(*b, s);
+    case RK_ETD34: return launch_evolve_ETD34(*b, s);
+    case RK_IF45DP: return launch_evolve_IF45DP(*b, s);
+    case RK_ETD4: return launch_evolve_ETD4(*b, s);
+    case RK_ETD5: return launch_evolve_ETD5(*b, s);
+    case RK_IF4: return launch_evolve_IF4(*b, s);
+  }
+  return RK_E_ARG;
+}
+
+}  // extern "C"

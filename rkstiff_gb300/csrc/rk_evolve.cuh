@@ -1,0 +1,613 @@
+// Persistent evolve kernel: one thread group per instance runs the reference's evolve
+// loop (rkstiff/solveras.py:556-650 or solvercs.py:191-279) entirely on the device.
+//
+// Per attempt: coefficients when h changed (FP64, rkstiff/etd35.py:842-855), the stage
+// program of the method with the built-in nonlinearity evaluated by in-shared-memory
+// FFTs, the masked error norm accumulated in FP64 (solveras.py:451-455), and the
+// accept/reject rule (solveras.py:384-410, 457-554).
+#pragma once
+
+#include "rk_coeffs.cuh"
+#include "rk_common.cuh"
+#include "rk_fft.cuh"
+
+namespace rk {
+
+// ---------------------------------------------------------------------------------
+// method traits: NN stage arrays N1..NN, NC coefficient arrays, order q
+// ---------------------------------------------------------------------------------
+template <int M> struct Traits;
+template <> struct Traits<RK_ETD35> { enum { NN = 6, NC = C35_N, Q = 4, ADAPT = 1, FSAL = 0 }; };
+template <> struct Traits<RK_ETD5> { enum { NN = 6, NC = C35_N, Q = 0, ADAPT = 0, FSAL = 0 }; };
+template <> struct Traits<RK_ETD34> { enum { NN = 5, NC = C34_N, Q = 4, ADAPT = 1, FSAL = 1 }; };
+template <> struct Traits<RK_ETD4> { enum { NN = 4, NC = C34_N, Q = 0, ADAPT = 0, FSAL = 0 }; };
+template <> struct Traits<RK_IF34> { enum { NN = 5, NC = CIF_N, Q = 4, ADAPT = 1, FSAL = 1 }; };
+template <> struct Traits<RK_IF4> { enum { NN = 4, NC = CIF_N, Q = 0, ADAPT = 0, FSAL = 0 }; };
+template <> struct Traits<RK_IF45DP> { enum { NN = 7, NC = CDP_N, Q = 5, ADAPT = 1, FSAL = 1 }; };
+
+RK_HD int64_t round_up4(int64_t m) { return (m + 3) & ~int64_t(3); }
+
+RK_HD int traits_nn(int method) {
+  switch (method) {
+    case RK_ETD35: case RK_ETD5: return 6;
+    case RK_ETD34: case RK_IF34: return 5;
+    case RK_ETD4: case RK_IF4: return 4;
+    case RK_IF45DP: return 7;
+  }
+  return 0;
+}
+
+// bytes of an instance's scratch: u, unew, N1..NN (complex T) and the coefficient block
+RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m) {
+  const int64_t mp = round_up4(m);
+  const int64_t ts = precision == RK_FP64 ? 8 : 4;
+  const int64_t vec = 2 * ts * mp;
+  const int64_t coef = (coef_complex ? 2 : 1) * ts * mp;
+  return (2 + traits_nn(method)) * vec + num_coeffs(method) * coef;
+}
+
+// ---------------------------------------------------------------------------------
+// per-instance working context
+// ---------------------------------------------------------------------------------
+template <class T, class CT>
+struct Ctx {
+  Group g;
+  int n, logn, m, mp, nl_kind;
+  T nl_c;
+  const double* kx;
+  const cx<double>* lin;
+  cx<T>* u;
+  cx<T>* unew;
+  cx<T>* N[8];
+  CT* C;
+  cx<T>* fa;
+  cx<T>* fb;
+  double* red;
+  const cx<T>* tw;
+  RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
+};
+
+// ---------------------------------------------------------------------------------
+// built-in nonlinearities: out[j] = N(k)[j] with k[j] = kf(j)
+// ---------------------------------------------------------------------------------
+template <class T, class CT, class KF>
+RK_DEV void nl_eval(const Ctx<T, CT>& x, KF kf, cx<T>* __restrict__ out) {
+  const Group& g = x.g;
+  if (x.nl_kind == RK_NL_UUX) {
+    // u = irfft(k), ux = irfft(i kx k) packed as one complex inverse FFT of length n:
+    // Z = A + iB with A, B the Hermitian spectra; numpy's irfft drops the imaginary
+    // parts of the DC and Nyquist bins, so they are dropped here too.
+    const int n = x.n, M = n >> 1;
+    const T inv_n = T(1) / T(n);
+    cx<T>* Z = x.fa;
+    for (int j = g.tid; j <= M; j += g.nthr) {
+      cx<T> k = kf(j);
+      cx<T> A = k * inv_n;
+      cx<T> B = mul_i(k) * (T(x.kx[j]) * inv_n);
+      if (j == 0 || j == M) {
+        A.y = T(0);
+        B.y = T(0);
+      }
+      Z[j] = cx<T>{A.x - B.y, A.y + B.x};
+      if (j > 0 && j < M) Z[n - j] = cx<T>{A.x + B.y, B.x - A.y};
+    }
+    g.sync();
+    cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
+    cx<T>* other = (z == x.fa) ? x.fb : x.fa;
+    T* w = reinterpret_cast<T*>(other);
+    for (int t = g.tid; t < n; t += g.nthr) {
+      cx<T> v = z[t];
+      w[t] = v.x * v.y;
+    }
+    g.sync();
+    // rfft of the real product via a complex FFT of length n/2 and the split formula
+    cx<T>* F = fft_group<T, false>(g, other, z, x.logn - 1, x.tw);
+    const int tws = RK_TW_N >> x.logn;
+    for (int k = g.tid; k <= M; k += g.nthr) {
+      cx<T> Fk = F[k == M ? 0 : k];
+      cx<T> Fm = conj(F[k == 0 ? 0 : M - k]);
+      cx<T> Fe = (Fk + Fm) * T(0.5);
+      cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+      cx<T> W = Fe + x.tw[k * tws] * Fo;
+      out[k] = W * x.nl_c;
+    }
+    g.sync();
+  } else if (x.nl_kind == RK_NL_NLS) {
+    // v = ifft(k); N = fft(i c |v|^2 v)
+    const int n = x.n;
+    const T inv_n = T(1) / T(n);
+    for (int j = g.tid; j < n; j += g.nthr) x.fa[j] = kf(j) * inv_n;
+    g.sync();
+    cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
+    cx<T>* other = (z == x.fa) ? x.fb : x.fa;
+    for (int t = g.tid; t < n; t += g.nthr) {
+      cx<T> v = z[t];
+      T a2 = (v.x * v.x + v.y * v.y) * x.nl_c;
+      other[t] = cx<T>{-a2 * v.y, a2 * v.x};
+    }
+    g.sync();
+    cx<T>* F = fft_group<T, false>(g, other, z, x.logn, x.tw);
+    for (int k = g.tid; k < n; k += g.nthr) out[k] = F[k];
+    g.sync();
+  } else {
+    for (int k = g.tid; k < x.m; k += g.nthr) out[k] = cx<T>{T(0), T(0)};
+    g.sync();
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// coefficients at step h (FP64 math), stored in the working precision
+// ---------------------------------------------------------------------------------
+template <class T> RK_DEV void store_c(T& d, double v) { d = T(v); }
+template <class T> RK_DEV void store_c(cx<T>& d, cx<double> v) { d = cx<T>{T(v.x), T(v.y)}; }
+
+template <class S> RK_DEV S load_z(const cx<double>* lin, int j, double h);
+template <> RK_DEV double load_z<double>(const cx<double>* lin, int j, double h) { return h * lin[j].x; }
+template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, double h) {
+  cx<double> L = lin[j];
+  return cx<double>{h * L.x, h * L.y};
+}
+
+// S: double for a real operator (CT real), cx<double> for a complex one.
+template <class T, class CT, class S, int METHOD>
+RK_DEV void compute_coeffs(const Ctx<T, CT>& x, double h, const EtdCfg& ec) {
+  const Group& g = x.g;
+  constexpr int NC = Traits<METHOD>::NC;
+  if (!is_etd(METHOD)) {
+    for (int j = g.tid; j < x.m; j += g.nthr) {
+      S z = load_z<S>(x.lin, j, h);
+      S o[NC];
+      if_coeffs<S>(METHOD, z, h, o);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+    }
+    g.sync();
+    return;
+  }
+  constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
+  // pass 1: thread per mode, direct formula for |z| >= modecutoff
+  for (int j = g.tid; j < x.m; j += g.nthr) {
+    S z = load_z<S>(x.lin, j, h);
+    if (sabs(z) < ec.cutoff) continue;
+    S P[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      int order;
+      double num, den;
+      psi_slot(METHOD, k, order, num, den);
+      P[k] = direct_hpsi(z, h, order, num, den);
+    }
+    S o[NC];
+    etd_from_psi<S>(METHOD, z, P, o);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+  }
+  // pass 2: warp per small mode, lanes over the contour nodes (rkstiff/etd35.py:257-288)
+  const int lane = g.tid & 31, warp = g.tid >> 5, nwarp = g.nthr >> 5;
+  for (int j = warp; j < x.m; j += nwarp) {
+    S z = load_z<S>(x.lin, j, h);
+    if (!(sabs(z) < ec.cutoff)) continue;
+    cx<double> zc = to_cx(z);
+    cx<double> acc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) acc[k] = cx<double>{0.0, 0.0};
+    for (int q = lane; q < ec.np; q += 32) {
+#pragma unroll
+      for (int k = 0; k < NP; ++k) {
+        int order;
+        double num, den;
+        psi_slot(METHOD, k, order, num, den);
+        acc[k] = acc[k] + contour_term(zc, ec, q, order, num, den);
+      }
+    }
+    S P[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      double re = warp_sum(acc[k].x), im = warp_sum(acc[k].y);
+      P[k] = from_cx<S>(rdiv(h * cx<double>{re, im}, (double)ec.np));
+    }
+    if (lane == 0) {
+      S o[NC];
+      etd_from_psi<S>(METHOD, z, P, o);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+    }
+  }
+  g.sync();
+}
+
+// ---------------------------------------------------------------------------------
+// new state + controller factor s (FP64 masked norms)
+// ---------------------------------------------------------------------------------
+template <class T> RK_DEV double cabs_d(cx<T> v) { return hypot((double)v.x, (double)v.y); }
+
+template <class T, class CT, class KF>
+RK_DEV double write_unew(const Ctx<T, CT>& x, KF kf) {
+  double mx = 0.0;
+  bool nan = false;
+  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+    cx<T> v = kf(j);
+    x.unew[j] = v;
+    double a = cabs_d(v);
+    if (a != a) nan = true;
+    else mx = fmax(mx, a);
+  }
+  return group_max_nan(x.g, x.red, nan ? nan_d() : mx);
+}
+
+template <class T, class CT, class EF>
+RK_DEV double controller_s(const Ctx<T, CT>& x, double maxu, EF ef, const rk_controller& ctl, int q) {
+  double su = 0.0, se = 0.0;
+  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+    cx<T> v = x.unew[j];
+    double a = cabs_d(v);
+    if (a / maxu > ctl.adapt_cutoff) {
+      su += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+      cx<T> e = ef(j);
+      se += (double)e.x * (double)e.x + (double)e.y * (double)e.y;
+    }
+  }
+  group_sum2(x.g, x.red, su, se);
+  double tol = ctl.epsilon * sqrt(su);
+  return ctl.safety_f * pow(tol / sqrt(se), 1.0 / q);
+}
+
+// ---------------------------------------------------------------------------------
+// stage programs.  Each computes N2.. and unew (and N(unew) where the method needs it)
+// and returns s (adaptive) or 0 (constant).  N1 must be valid on entry.
+// ---------------------------------------------------------------------------------
+template <class T, class CT>
+RK_DEV double attempt_etd35_family(const Ctx<T, CT>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
+  const cx<T>* u = x.u;
+  cx<T>* const* N = x.N;
+  // rkstiff/etd35.py:320-345 (ETD5: etd5.py:236-260)
+  nl_eval(x, [&](int j) { return cmul(x.c(C35_E14, j), u[j]) + cmul(x.c(C35_A21, j), N[0][j]); }, N[1]);
+  nl_eval(x, [&](int j) {
+    return (cmul(x.c(C35_E14, j), u[j]) + cmul(x.c(C35_A31, j), N[0][j])) + cmul(x.c(C35_A32, j), N[1][j]);
+  }, N[2]);
+  nl_eval(x, [&](int j) {
+    return (cmul(x.c(C35_E12, j), u[j]) + cmul(x.c(C35_A41, j), N[0][j])) + cmul(x.c(C35_A43, j), N[2][j]);
+  }, N[3]);
+  nl_eval(x, [&](int j) {
+    return ((cmul(x.c(C35_E34, j), u[j]) + cmul(x.c(C35_A51, j), N[0][j])) + cmul(x.c(C35_A52, j), N[1][j] - N[2][j])) +
+           cmul(x.c(C35_A54, j), N[3][j]);
+  }, N[4]);
+  nl_eval(x, [&](int j) {
+    cx<T> t = N[1][j] - (T(3) * N[3][j]) * T(0.5);
+    return (((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A61, j), N[0][j])) + cmul(x.c(C35_A62, j), t)) +
+            cmul(x.c(C35_A63, j), N[2][j])) + cmul(x.c(C35_A65, j), N[4][j]);
+  }, N[5]);
+  nl_count += 5;
+  auto k7 = [&](int j) {
+    return ((((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A71, j), N[0][j])) + cmul(x.c(C35_A73, j), N[2][j])) +
+             cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) + cmul(x.c(C35_A76, j), N[5][j]);
+  };
+  if (!adaptive) {
+    // ETD5: unew, then N1 <- N(unew) (FSAL, etd5.py:260)
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7(j);
+    x.g.sync();
+    const cx<T>* un = x.unew;
+    nl_eval(x, [&](int j) { return un[j]; }, N[0]);
+    nl_count += 1;
+    return 0.0;
+  }
+  double mx = write_unew(x, k7);
+  return controller_s(x, mx, [&](int j) {
+    cx<T> s = (((-N[0][j] + T(4) * N[2][j]) - T(6) * N[3][j]) + T(4) * N[4][j]) - N[5][j];
+    return cmul(x.c(C35_A75, j), s);
+  }, ctl, 4);
+}
+
+template <class T, class CT>
+RK_DEV double attempt_etd34_family(const Ctx<T, CT>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
+  const cx<T>* u = x.u;
+  cx<T>* const* N = x.N;
+  // rkstiff/etd34.py:182-190 (ETD4: etd4.py:167-174)
+  nl_eval(x, [&](int j) { return cmul(x.c(C34_E2, j), u[j]) + cmul(x.c(C34_A21, j), N[0][j]); }, N[1]);
+  nl_eval(x, [&](int j) {
+    return (cmul(x.c(C34_E2, j), u[j]) + cmul(x.c(C34_A31, j), N[0][j])) + cmul(x.c(C34_A32, j), N[1][j]);
+  }, N[2]);
+  nl_eval(x, [&](int j) {
+    return (cmul(x.c(C34_E, j), u[j]) + cmul(x.c(C34_A41, j), N[0][j])) + cmul(x.c(C34_A43, j), N[2][j]);
+  }, N[3]);
+  nl_count += 3;
+  auto k5 = [&](int j) {
+    return ((cmul(x.c(C34_E, j), u[j]) + cmul(x.c(C34_A51, j), N[0][j])) + cmul(x.c(C34_A52, j), N[1][j] + N[2][j])) +
+           cmul(x.c(C34_A54, j), N[3][j]);
+  };
+  const cx<T>* un = x.unew;
+  if (!adaptive) {
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k5(j);
+    x.g.sync();
+    nl_eval(x, [&](int j) { return un[j]; }, N[0]);
+    nl_count += 1;
+    return 0.0;
+  }
+  double mx = write_unew(x, k5);
+  nl_eval(x, [&](int j) { return un[j]; }, N[4]);
+  nl_count += 1;
+  return controller_s(x, mx, [&](int j) { return cmul(x.c(C34_A54, j), N[3][j] - N[4][j]); }, ctl, 4);
+}
+
+template <class T, class CT>
+RK_DEV double attempt_if34_family(const Ctx<T, CT>& x, double hd, bool adaptive, const rk_controller& ctl,
+                                  int& nl_count) {
+  const cx<T>* u = x.u;
+  cx<T>* const* N = x.N;
+  const T h = T(hd);
+  const T r6 = T(1.0 / 6.0), r3 = T(1.0 / 3.0);
+  // rkstiff/if34.py:120-130 (IF4: if4.py:112-121)
+  nl_eval(x, [&](int j) { return cmul(x.c(CIF_E2, j), u[j]) + cmul(h * x.c(CIF_E2, j), N[0][j]) * T(0.5); }, N[1]);
+  nl_eval(x, [&](int j) { return cmul(x.c(CIF_E2, j), u[j]) + (h * N[1][j]) * T(0.5); }, N[2]);
+  nl_eval(x, [&](int j) { return cmul(x.c(CIF_E, j), u[j]) + cmul(h * x.c(CIF_E2, j), N[2][j]); }, N[3]);
+  nl_count += 3;
+  auto k5 = [&](int j) {
+    cx<T> s = ((cmul(x.c(CIF_E, j), N[0][j]) * r6 + cmul(x.c(CIF_E2, j), N[1][j]) * r3) +
+               cmul(x.c(CIF_E2, j), N[2][j]) * r3) + N[3][j] * r6;
+    return cmul(x.c(CIF_E, j), u[j]) + h * s;
+  };
+  const cx<T>* un = x.unew;
+  if (!adaptive) {
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k5(j);
+    x.g.sync();
+    nl_eval(x, [&](int j) { return un[j]; }, N[0]);
+    nl_count += 1;
+    return 0.0;
+  }
+  double mx = write_unew(x, k5);
+  nl_eval(x, [&](int j) { return un[j]; }, N[4]);
+  nl_count += 1;
+  return controller_s(x, mx, [&](int j) { return (h * (N[3][j] - N[4][j])) * r6; }, ctl, 4);
+}
+
+template <class T, class CT>
+RK_DEV double attempt_if45dp(const Ctx<T, CT>& x, double hd, const rk_controller& ctl, int& nl_count) {
+  const cx<T>* u = x.u;
+  cx<T>* const* N = x.N;
+  const T a76 = T(dp_a76(hd)), r6 = T(dp_r6(hd)), r7 = T(dp_r7(hd));
+  // rkstiff/if45dp.py:140-179
+  nl_eval(x, [&](int j) { return cmul(x.c(CDP_E15, j), u[j]) + cmul(x.c(CDP_A21, j), N[0][j]); }, N[1]);
+  nl_eval(x, [&](int j) {
+    return (cmul(x.c(CDP_E310, j), u[j]) + cmul(x.c(CDP_A31, j), N[0][j])) + cmul(x.c(CDP_A32, j), N[1][j]);
+  }, N[2]);
+  nl_eval(x, [&](int j) {
+    return ((cmul(x.c(CDP_E45, j), u[j]) + cmul(x.c(CDP_A41, j), N[0][j])) + cmul(x.c(CDP_A42, j), N[1][j])) +
+           cmul(x.c(CDP_A43, j), N[2][j]);
+  }, N[3]);
+  nl_eval(x, [&](int j) {
+    return (((cmul(x.c(CDP_E89, j), u[j]) + cmul(x.c(CDP_A51, j), N[0][j])) + cmul(x.c(CDP_A52, j), N[1][j])) +
+            cmul(x.c(CDP_A53, j), N[2][j])) + cmul(x.c(CDP_A54, j), N[3][j]);
+  }, N[4]);
+  nl_eval(x, [&](int j) {
+    return ((((cmul(x.c(CDP_E, j), u[j]) + cmul(x.c(CDP_A61, j), N[0][j])) + cmul(x.c(CDP_A62, j), N[1][j])) +
+             cmul(x.c(CDP_A63, j), N[2][j])) + cmul(x.c(CDP_A64, j), N[3][j])) + cmul(x.c(CDP_A65, j), N[4][j]);
+  }, N[5]);
+  nl_count += 5;
+  auto k7 = [&](int j) {
+    return ((((cmul(x.c(CDP_E, j), u[j]) + cmul(x.c(CDP_A71, j), N[0][j])) + cmul(x.c(CDP_A73, j), N[2][j])) +
+             cmul(x.c(CDP_A74, j), N[3][j])) + cmul(x.c(CDP_A75, j), N[4][j])) + a76 * N[5][j];
+  };
+  double mx = write_unew(x, k7);
+  const cx<T>* un = x.unew;
+  nl_eval(x, [&](int j) { return un[j]; }, N[6]);
+  nl_count += 1;
+  return controller_s(x, mx, [&](int j) {
+    return ((((cmul(x.c(CDP_R1, j), N[0][j]) + cmul(x.c(CDP_R3, j), N[2][j])) + cmul(x.c(CDP_R4, j), N[3][j])) +
+             cmul(x.c(CDP_R5, j), N[4][j])) + r6 * N[5][j]) + r7 * N[6][j];
+  }, ctl, 5);
+}
+
+template <class T, class CT, int METHOD>
+RK_DEV double run_attempt(const Ctx<T, CT>& x, double h, const rk_controller& ctl, int& nl_count) {
+  switch (METHOD) {
+    case RK_ETD35: return attempt_etd35_family(x, true, ctl, nl_count);
+    case RK_ETD5: return attempt_etd35_family(x, false, ctl, nl_count);
+    case RK_ETD34: return attempt_etd34_family(x, true, ctl, nl_count);
+    case RK_ETD4: return attempt_etd34_family(x, false, ctl, nl_count);
+    case RK_IF34: return attempt_if34_family(x, h, true, ctl, nl_count);
+    case RK_IF4: return attempt_if34_family(x, h, false, ctl, nl_count);
+    case RK_IF45DP: return attempt_if45dp(x, h, ctl, nl_count);
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------------
+// step-size rules (rkstiff/solveras.py:492-554); class constants MIN_S, MAX_S, MAX_LOOPS
+// ---------------------------------------------------------------------------------
+RK_DEV double reject_h(double s, double h, const rk_controller& c) {
+  if (isinf(s) || isnan(s)) return 0.25 * h;
+  s = fmax(s, 0.25);
+  s = fmin(s, c.decr_f);
+  return s * h;
+}
+RK_DEV double accept_h(double s, double h, const rk_controller& c) {
+  s = fmin(s, 4.0);
+  return s > c.incr_f ? s * h : h;
+}
+
+// ---------------------------------------------------------------------------------
+// one instance, start to pause/finish
+// ---------------------------------------------------------------------------------
+template <class T, class CT, class S, int METHOD>
+RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red) {
+  using Tr = Traits<METHOD>;
+  Ctx<T, CT> x;
+  x.g = g;
+  x.n = b.n[inst];
+  x.logn = 31 - __clz(x.n);
+  x.nl_kind = b.nl_kind;
+  x.m = (b.nl_kind == RK_NL_UUX) ? (x.n / 2 + 1) : x.n;
+  x.mp = (int)round_up4(x.m);
+  x.nl_c = T(b.nl_coef);
+  const int64_t mo = b.mode_off[inst];
+  x.kx = b.kx ? b.kx + mo : nullptr;
+  x.lin = reinterpret_cast<const cx<double>*>(b.lin_op) + mo;
+  cx<T>* sl = reinterpret_cast<cx<T>*>(reinterpret_cast<char*>(b.slab) + b.slab_off[inst]);
+  x.u = sl;
+  x.unew = sl + x.mp;
+  for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? sl + (2 + i) * x.mp : nullptr;
+  x.C = reinterpret_cast<CT*>(sl + (2 + Tr::NN) * x.mp);
+  x.fa = fa;
+  x.fb = fb;
+  x.red = red;
+  x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
+  const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
+  const rk_controller ctl = b.ctl;
+
+  rk_inst_state st = b.state[inst];
+  // only RUNNING instances step; finished or failed ones keep their record untouched
+  if (st.status != RK_ST_RUNNING) return;
+  cx<T>* uio = reinterpret_cast<cx<T>*>(b.u) + mo;
+  for (int j = g.tid; j < x.m; j += g.nthr) x.u[j] = uio[j];
+  g.sync();
+
+  double t = st.t, tf = st.tf, h = st.h, hc = st.h_coeff;
+  bool accept = st.accept != 0;
+  bool n1_valid = false;
+  const bool resumed = st.steps > 0;
+  int status = RK_ST_RUNNING;
+  int64_t steps_this = 0;
+  int snap = 0;
+  int64_t attempts = 0, rejects = 0, nl_evals = 0, coeff_updates = 0;
+  double s_last = st.s_last, h_used = st.h_used, h_sug = st.h_suggest;
+
+  if (b.run_mode == RK_RUN_EVOLVE && !(t < tf)) status = RK_ST_DONE;
+  while (status == RK_ST_RUNNING) {
+    if (Tr::ADAPT) {
+      int numloops = 0;
+      double hs = h;
+      for (;;) {
+        if (h != hc) {  // exact compare, as the reference's _update_coeffs
+          compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+          hc = h;
+          ++coeff_updates;
+        }
+        int nlc = 0;
+        if (!n1_valid || (METHOD == RK_ETD35 && accept)) {
+          const cx<T>* uu = x.u;
+          nl_eval(x, [&](int j) { return uu[j]; }, x.N[0]);
+          // an FSAL method resuming mid-run re-derives N1 = N(u); it is not a new evaluation
+          if (!(resumed && !n1_valid && Tr::FSAL)) ++nlc;
+          n1_valid = true;
+        }
+        double s = run_attempt<T, CT, METHOD>(x, h, ctl, nlc);
+        nl_evals += nlc;
+        ++attempts;
+        s_last = s;
+        if (isinf(s) || isnan(s) || s < 1.0) {
+          accept = false;
+          ++rejects;
+          h = reject_h(s, h, ctl);
+          ++numloops;
+          if (numloops > 50) { status = RK_ST_MAX_LOOPS; break; }
+          if (h < ctl.minh) { status = RK_ST_MIN_STEP; break; }
+        } else {
+          accept = true;
+          hs = accept_h(s, h, ctl);
+          break;
+        }
+      }
+      if (status != RK_ST_RUNNING) break;
+      // accepted: u <- unew; FSAL methods carry N(unew) into N1
+      { cx<T>* tmp = x.u; x.u = x.unew; x.unew = tmp; }
+      if (Tr::FSAL) { cx<T>* tmp = x.N[0]; x.N[0] = x.N[Tr::NN - 1]; x.N[Tr::NN - 1] = tmp; }
+      t += h;
+      h_used = h;
+      h_sug = hs;
+      h = (t + hs > tf) ? tf - t : hs;
+    } else {
+      if (h != hc) {
+        compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+        hc = h;
+        ++coeff_updates;
+      }
+      int nlc = 0;
+      if (!n1_valid) {
+        const cx<T>* uu = x.u;
+        nl_eval(x, [&](int j) { return uu[j]; }, x.N[0]);
+        if (!resumed) ++nlc;
+        n1_valid = true;
+      }
+      run_attempt<T, CT, METHOD>(x, h, ctl, nlc);
+      nl_evals += nlc;
+      ++attempts;
+      { cx<T>* tmp = x.u; x.u = x.unew; x.unew = tmp; }
+      t += h;
+      h_used = h;
+    }
+    ++st.steps;
+    ++steps_this;
+    if (b.store_freq > 0 && (st.steps % b.store_freq) == 0 && snap < b.snap_cap) {
+      cx<T>* su = reinterpret_cast<cx<T>*>(b.snap_u) + (int64_t)b.snap_cap * mo + (int64_t)snap * x.m;
+      for (int j = g.tid; j < x.m; j += g.nthr) su[j] = x.u[j];
+      if (g.tid == 0) b.snap_t[(int64_t)inst * b.snap_cap + snap] = t;
+      ++snap;
+    }
+    if (b.run_mode == RK_RUN_STEP) status = RK_ST_STEP_DONE;
+    else if (!(t < tf)) status = RK_ST_DONE;
+    else if (b.store_freq > 0 && snap >= b.snap_cap) status = RK_ST_SNAP_FULL;
+    else if (steps_this >= b.max_steps) status = RK_ST_ITER_CAP;
+  }
+  g.sync();
+  for (int j = g.tid; j < x.m; j += g.nthr) uio[j] = x.u[j];
+  if (g.tid == 0) {
+    st.t = t;
+    st.h = h;
+    st.h_coeff = hc;
+    st.h_used = h_used;
+    st.h_suggest = h_sug;
+    st.s_last = s_last;
+    st.status = status;
+    st.accept = accept ? 1 : 0;
+    st.snap_count = snap;
+    st.attempts += attempts;
+    st.rejects += rejects;
+    st.nl_evals += nl_evals;
+    st.coeff_updates += coeff_updates;
+    b.state[inst] = st;
+  }
+  // The swapped u/unew roles mean the slab's first array may no longer hold u; only the
+  // copy in `uio` is authoritative between launches, so nothing else is persisted.
+  g.sync();
+}
+
+template <class T, class CT, class S, int METHOD>
+__global__ void __launch_bounds__(256, 1) evolve_kernel(const rk_batch b, int nfft) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  cx<T>* fa = reinterpret_cast<cx<T>*>(smem);
+  cx<T>* fb = fa + nfft;
+  double* red = reinterpret_cast<double*>(fb + nfft);
+  int* item_s = reinterpret_cast<int*>(red + 64);
+  Group g{(int)threadIdx.x, (int)blockDim.x, 0};
+  for (;;) {
+    if (g.tid == 0) *item_s = atomicAdd(b.queue, 1);
+    g.sync();
+    const int item = *item_s;
+    g.sync();
+    if (item >= b.n_inst) break;
+    const int inst = b.order ? b.order[item] : item;
+    run_instance<T, CT, S, METHOD>(b, inst, g, fa, fb, red);
+  }
+}
+
+template <class T, class CT, class S, int METHOD>
+__global__ void coeff_kernel(int m, const double* lin, double h, rk_etd_config etd, CT* out) {
+  // standalone coefficient evaluation for one operator (blocks split the modes)
+  Ctx<T, CT> x;
+  x.g = Group{(int)threadIdx.x, (int)blockDim.x, 0};
+  const int per = blockDim.x;
+  const int j0 = blockIdx.x * per;
+  x.m = min(per, m - j0);
+  x.mp = m;  // arrays of length m, shifted so that c*mp + j addresses mode j0 + j
+  x.lin = reinterpret_cast<const cx<double>*>(lin) + j0;
+  x.C = out + j0;
+  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points};
+  compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+}
+
+// smem bytes of the evolve kernel for complex FFT length nfft
+template <class T> inline size_t evolve_smem(int nfft) {
+  return 2 * (size_t)nfft * sizeof(cx<T>) + 64 * sizeof(double) + 16;
+}
+
+}  // namespace rk

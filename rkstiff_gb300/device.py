@@ -1,0 +1,26 @@
+"""Device-side options shared by all solvers (not part of the reference API)."""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Optional, Union
+
+import torch
+
+
+@dataclass
+class DeviceOptions:
+    """How a solver runs on the GPU.
+
+    precision : 'fp64' (complex128 stages, the reference's arithmetic) or 'fp32'
+                (complex64 stages and FFTs; coefficients still built in FP64, error norm
+                accumulated in FP64, time kept in FP64)
+    device    : CUDA device (default: the current one)
+    threads   : threads per instance group (0: the kernel default, 256)
+    snap_cap  : snapshots the device buffers hold before the host drains them
+    """
+
+    precision: str = "fp64"
+    device: Optional[Union[str, torch.device]] = None
+    threads: int = 0
+    snap_cap: int = 256

@@ -1,0 +1,53 @@
+"""Grid builders used to set up problems (host-side, one-time; the same grids as
+rkstiff/grids.py:40-219)."""
+
+from __future__ import annotations
+
+from typing import Tuple
+
+import numpy as np
+
+
+def _check_even(n):
+    if not isinstance(n, (int, np.integer)):
+        raise TypeError("n must be an integer.")
+    if n <= 2 or (n % 2) != 0:
+        raise ValueError("n must be an even integer greater than 2.")
+
+
+def construct_x_kx_rfft(n: int, a: float = 0.0, b: float = 2 * np.pi) -> Tuple[np.ndarray, np.ndarray]:
+    """Uniform grid on [a, b) and its real-FFT wavenumbers (length n/2 + 1)."""
+    _check_even(n)
+    dx = (b - a) / n
+    x = np.arange(a, b, dx)
+    return x, 2 * np.pi * np.fft.rfftfreq(n, d=dx)
+
+
+def construct_x_kx_fft(n: int, a: float = 0.0, b: float = 2 * np.pi) -> Tuple[np.ndarray, np.ndarray]:
+    """Uniform grid on [a, b) and its complex-FFT wavenumbers (length n)."""
+    _check_even(n)
+    dx = (b - a) / n
+    x = np.arange(a, b, dx)
+    return x, 2 * np.pi * np.fft.fftfreq(n, d=dx)
+
+
+def construct_x_cheb(n: int, a: float = -1.0, b: float = 1.0) -> np.ndarray:
+    """n + 1 Chebyshev extreme points mapped to [a, b]."""
+    if not isinstance(n, (int, np.integer)):
+        raise TypeError("n must be an integer.")
+    if n < 2:
+        raise ValueError("n must be >= 2.")
+    x = np.polynomial.chebyshev.chebpts2(n + 1)
+    return a + (b - a) * (x + 1) / 2.0
+
+
+def construct_x_dx_cheb(n: int, a: float = -1, b: float = 1) -> Tuple[np.ndarray, np.ndarray]:
+    """Chebyshev points and the (n+1) x (n+1) first-derivative matrix (negative-sum trick
+    on the diagonal)."""
+    x = construct_x_cheb(n, a, b)
+    c = np.r_[2, np.ones(n - 1), 2] * np.power(-1, np.arange(0, n + 1))
+    X = np.tile(x.reshape(n + 1, 1), (1, n + 1))
+    dX = X - X.T
+    D = np.outer(c, 1.0 / c) / (dX + np.eye(n + 1))
+    D = D - np.diag(D.sum(axis=1))
+    return x, D

@@ -1,0 +1,107 @@
+"""Model equations whose nonlinearities run as fused device kernels.
+
+Each ``*_ops`` helper returns ``(lin_op, nl_func)`` like rkstiff/models.py does, but
+``nl_func`` is a :class:`BuiltinNL`: a callable that also tells the solvers which fused
+kernel to run.  Calling it directly evaluates the same map with torch (on the device of a
+tensor argument), which is also what the host-driven path for user callables uses.
+"""
+
+from __future__ import annotations
+
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _native as nat
+
+
+class BuiltinNL:
+    """A nonlinearity with a fused device implementation.
+
+    kind  : RK_NL_UUX  -> c * rfft(irfft(u) * irfft(i kx u))   (real grid, n points)
+            RK_NL_NLS  -> fft(i c |ifft(u)|^2 ifft(u))          (complex grid, n points)
+            RK_NL_NONE -> 0
+    """
+
+    def __init__(self, kind: int, coef: float, n: int, kx: Optional[np.ndarray] = None, name: str = ""):
+        self.kind = int(kind)
+        self.coef = float(coef)
+        self.n = int(n)
+        self.kx = None if kx is None else np.asarray(kx, dtype=np.float64)
+        self.name = name or {nat.RK_NL_UUX: "uux", nat.RK_NL_NLS: "nls", nat.RK_NL_NONE: "zero"}[self.kind]
+        self._kx_t = {}
+
+    @property
+    def modes(self) -> int:
+        return self.n // 2 + 1 if self.kind == nat.RK_NL_UUX else self.n
+
+    def _kx(self, device, dtype):
+        key = (str(device), dtype)
+        if key not in self._kx_t:
+            self._kx_t[key] = torch.as_tensor(self.kx, dtype=dtype, device=device)
+        return self._kx_t[key]
+
+    def torch_eval(self, u: torch.Tensor) -> torch.Tensor:
+        if self.kind == nat.RK_NL_UUX:
+            rdt = torch.float64 if u.dtype == torch.complex128 else torch.float32
+            kx = self._kx(u.device, rdt)
+            a = torch.fft.irfft(u, n=self.n)
+            b = torch.fft.irfft(1j * kx * u, n=self.n)
+            return self.coef * torch.fft.rfft(a * b)
+        if self.kind == nat.RK_NL_NLS:
+            v = torch.fft.ifft(u)
+            return torch.fft.fft(1j * self.coef * (v.abs() ** 2) * v)
+        return torch.zeros_like(u)
+
+    def __call__(self, u):
+        if isinstance(u, torch.Tensor):
+            return self.torch_eval(u)
+        t = torch.from_numpy(np.asarray(u, dtype=np.complex128))
+        return self.torch_eval(t).numpy()
+
+    def __repr__(self):
+        return f"BuiltinNL({self.name}, coef={self.coef}, n={self.n})"
+
+
+def _n_from_rfft_kx(kx) -> int:
+    return 2 * (len(kx) - 1)
+
+
+def ks_ops(kx: np.ndarray) -> Tuple[np.ndarray, BuiltinNL]:
+    """Kuramoto-Sivashinsky: L = kx^2 (1 - kx^2), N = -rfft(u u_x) (README quickstart)."""
+    kx = np.asarray(kx, dtype=np.float64)
+    return kx**2 * (1 - kx**2), BuiltinNL(nat.RK_NL_UUX, -1.0, _n_from_rfft_kx(kx), kx, "ks")
+
+
+def kdv_ops(kx: np.ndarray) -> Tuple[np.ndarray, BuiltinNL]:
+    """KdV: L = i kx^3, N = -6 rfft(u u_x) (rkstiff/models.py:113-145)."""
+    kx = np.asarray(kx, dtype=np.float64)
+    return 1j * kx**3, BuiltinNL(nat.RK_NL_UUX, -6.0, _n_from_rfft_kx(kx), kx, "kdv")
+
+
+def burgers_ops(kx: np.ndarray, mu: float) -> Tuple[np.ndarray, BuiltinNL]:
+    """Viscous Burgers: L = -mu kx^2, N = -rfft(u u_x) (rkstiff/models.py:153-194)."""
+    kx = np.asarray(kx, dtype=np.float64)
+    return -mu * kx**2, BuiltinNL(nat.RK_NL_UUX, -1.0, _n_from_rfft_kx(kx), kx, "burgers")
+
+
+def nls_ops(kx: np.ndarray, coef: float = 1.0) -> Tuple[np.ndarray, BuiltinNL]:
+    """Cubic NLS on a complex grid: L = -(i/2) kx^2, N = fft(i c |u|^2 u)."""
+    kx = np.asarray(kx, dtype=np.float64)
+    return -0.5j * kx**2, BuiltinNL(nat.RK_NL_NLS, coef, len(kx), None, "nls")
+
+
+def kdv_soliton(x: np.ndarray, ampl: float = 0.5, x0: float = 0.0, t: float = 0.0) -> np.ndarray:
+    """Exact KdV soliton (rkstiff/models.py:32-73)."""
+    return 0.5 * ampl**2 / (np.cosh(ampl * (x - x0 - ampl**2 * t) / 2) ** 2)
+
+
+def kdv_multi_soliton(x: np.ndarray, ampl: Sequence[float], x0: Sequence[float], t: float = 0.0) -> np.ndarray:
+    """Sum of KdV solitons (rkstiff/models.py:76-110)."""
+    if len(x0) != len(ampl):
+        raise ValueError("Lengths of ampl and x0 must match.")
+    a = np.asarray(ampl, dtype=float).reshape(1, -1)
+    c = np.asarray(x0, dtype=float).reshape(1, -1)
+    xx = np.asarray(x).reshape(-1, 1)
+    return np.sum(0.5 * a**2 / (np.cosh(a * (xx - c - a**2 * t) / 2) ** 2), axis=1)

@@ -1,0 +1,92 @@
+"""The C-ABI library builds, loads without a GPU and exports every declared symbol;
+the ctypes mirrors of the header's structs have the C layout."""
+
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from rkstiff_gb300 import _build, _native as nat
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "rkstiff_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(rk_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return nat.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert set(names) == set(nat.EXPORTS)
+    out = subprocess.run(["nm", "-D", "--defined-only", _build.lib_path()], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (rk_\w+)", out))
+    for n in names:
+        assert n in exported, n
+        assert hasattr(lib, n)
+
+
+def test_abi_version_and_sizes(lib):
+    assert lib.rk_abi_version() == 1
+    assert lib.rk_num_coeffs(nat.RK_ETD35) == 21
+    assert lib.rk_num_coeffs(nat.RK_ETD34) == 10
+    assert lib.rk_num_coeffs(nat.RK_IF34) == 2
+    assert lib.rk_num_coeffs(nat.RK_IF45DP) == 28
+    assert lib.rk_num_coeffs(99) < 0
+    # ETD35, FP32, real coefficients, m=513 -> mp=516: 8 complex arrays + 21 real arrays
+    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 0, 513) == 8 * 8 * 516 + 21 * 4 * 516
+    assert lib.rk_slab_bytes(nat.RK_IF34, nat.RK_FP64, 1, 100) == 7 * 16 * 100 + 2 * 16 * 100
+    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP64, 0, 0) < 0
+
+
+def test_argument_errors_without_gpu(lib):
+    b = nat.RkBatch()
+    b.method = 42
+    assert lib.rk_evolve(ctypes.byref(b), None) == -1
+    assert b"unknown method" in lib.rk_last_error()
+    assert lib.rk_evolve(None, None) == -1
+    b.method = nat.RK_ETD35
+    b.precision = 7
+    assert lib.rk_evolve(ctypes.byref(b), None) == -1
+    b.precision = nat.RK_FP32
+    b.n_inst = 0
+    assert lib.rk_evolve(ctypes.byref(b), None) == 0  # nothing to do
+
+
+def test_struct_layout_matches_c():
+    """Compile a C probe against the header and compare sizeof/offsetof with ctypes."""
+    fields = [f for f, _ in nat.RkBatch._fields_]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){",
+             'printf("%zu %zu %zu %zu\\n", sizeof(rk_batch), sizeof(rk_inst_state), sizeof(rk_controller),'
+             ' sizeof(rk_etd_config));']
+    for f in fields:
+        lines.append(f'printf("%zu\\n", offsetof(rk_batch, {f}));')
+    for f in nat.STATE_DTYPE.names:
+        lines.append(f'printf("%zu\\n", offsetof(rk_inst_state, {f}));')
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        exe = os.path.join(d, "probe")
+        open(c, "w").write("\n".join(lines))
+        subprocess.run(["gcc", "-O0", c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    vals = [int(v) for v in out]
+    assert vals[0] == ctypes.sizeof(nat.RkBatch)
+    assert vals[1] == nat.STATE_DTYPE.itemsize
+    assert vals[2] == ctypes.sizeof(nat.RkController)
+    assert vals[3] == ctypes.sizeof(nat.RkEtdConfig)
+    offs = vals[4:4 + len(fields)]
+    for f, o in zip(fields, offs):
+        assert getattr(nat.RkBatch, f).offset == o, f
+    soffs = vals[4 + len(fields):]
+    for f, o in zip(nat.STATE_DTYPE.names, soffs):
+        assert nat.STATE_DTYPE.fields[f][1] == o, f
