@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Throughput of the batched uneven Kuramoto-Sivashinsky ensemble (the headline workload).
+
+Workload: 4096 independent KS instances, grid n uniform over {256, 512, 1024, 2048},
+domain length L ~ U[22, 120], u0 = sum_{k=1..8} a_k cos(2 pi k x/L + phi_k) with
+a_k ~ N(0,1) exp(-k/4), phi_k ~ U[0, 2 pi); ETD35 adaptive (epsilon = 1e-5) with every
+instance stepping its own dt to tf = 100, FP32 stages (FP64 coefficients, error norm and
+time).  One bench step = the whole ensemble evolved from t = 0 to tf in one persistent
+launch.  Metric: mode-steps/s = sum_i m_i * accepted_steps_i / seconds (m_i = n_i/2 + 1).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's NumPy algorithm on this
+machine's host cores (a bounded sample of the same workload per step).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "workload": "ks_uneven_ensemble_etd35",
+    "instances": 4096,
+    "n_choices": [256, 512, 1024, 2048],
+    "L_range": [22.0, 120.0],
+    "ic_modes": 8,
+    "epsilon": 1e-5,
+    "tf": 100.0,
+    "method": "ETD35",
+    "seed": 20261203,
+}
+METRIC = "mode-steps/s (KS uneven ensemble, ETD35 eps=1e-5, tf=100)"
+UNIT = "mode-steps/s"
+
+
+def make_instances(count: int, seed: int):
+    """(n, L, u0_hat) per instance, seeded."""
+    rng = np.random.default_rng(seed)
+    ns = rng.choice(np.array(WORKLOAD["n_choices"]), size=count)
+    Ls = rng.uniform(*WORKLOAD["L_range"], size=count)
+    k = np.arange(1, WORKLOAD["ic_modes"] + 1)
+    amps = rng.standard_normal((count, k.size)) * np.exp(-k / 4.0)
+    phis = rng.uniform(0.0, 2 * np.pi, size=(count, k.size))
+    out = []
+    for i in range(count):
+        n, L = int(ns[i]), float(Ls[i])
+        x = np.arange(n) * (L / n)
+        u0 = np.sum(amps[i][:, None] * np.cos(2 * np.pi * k[:, None] * x[None, :] / L + phis[i][:, None]), axis=0)
+        out.append((n, L, np.fft.rfft(u0)))
+    return out
+
+
+def ks_operator(n: int, L: float):
+    kx = 2 * np.pi * np.fft.rfftfreq(n, d=L / n)
+    return kx, kx**2 * (1 - kx**2)
+
+
+# ------------------------------------------------------------------------------------
+# CPU baseline: the oracle (NumPy restatement of the reference algorithm), one instance
+# per worker process, all host cores
+# ------------------------------------------------------------------------------------
+def _cpu_instance(args):
+    n, L, u0 = args
+    from oracle import rk_oracle as O
+
+    kx, lin = ks_operator(n, L)
+
+    def nl(u):
+        return -np.fft.rfft(np.fft.irfft(u) * np.fft.irfft(1j * kx * u))
+
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=WORKLOAD["epsilon"]))
+    status = 0
+    try:
+        s.evolve(u0, 0.0, WORKLOAD["tf"], store_data=False)
+    except (O.MinimumStepReached, O.MaxLoopsExceeded):
+        status = 1
+    steps = sum(1 for r in s.log if r[3])
+    return n // 2 + 1, steps, s.attempts, status
+
+
+def cpu_pool(cores: int):
+    for var in ("OMP_NUM_THREADS", "MKL_NUM_THREADS", "OPENBLAS_NUM_THREADS"):
+        os.environ[var] = "1"
+    return mp.get_context("spawn").Pool(cores)
+
+
+def cpu_measure(pool, sample):
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_instance, sample, chunksize=1)
+    wall = time.perf_counter() - t0
+    mode_steps = sum(m * s for m, s, _, _ in res)
+    return mode_steps / wall, wall, res
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [p.strip() for p in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+def flops_of(ens_engine, st) -> float:
+    """Algorithmic FP32 FLOPs of one launch from its counters: per nonlinear evaluation
+    7.5 n log2 n + n + 2m (one complex inverse FFT of n, one forward of n/2, the product
+    and the packing), 215 m per attempt (stage combinations and the error norm)."""
+    n = ens_engine.ns.astype(np.float64)
+    m = ens_engine.ms.astype(np.float64)
+    per_nl = 7.5 * n * np.log2(n) + n + 2 * m
+    return float(np.sum(st["nl_evals"] * per_nl + st["attempts"] * 215.0 * m))
+
+
+def measure_fp32_peak(device) -> float:
+    import torch
+
+    from rkstiff_gb300 import _native as nat
+
+    lib = nat.load()
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks, threads, iters = nsm * 8, 256, 1 << 15
+    out = torch.empty(blocks * threads, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+    for _ in range(2):
+        nat.check(lib.rk_probe_fp32(out.data_ptr(), blocks, threads, iters, stream.cuda_stream), "probe")
+    best = 0.0
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        nat.check(lib.rk_probe_fp32(out.data_ptr(), blocks, threads, iters, stream.cuda_stream), "probe")
+        e1.record(stream)
+        e1.synchronize()
+        best = max(best, 16.0 * blocks * threads * iters / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+def gpu_arm(args, rank, world, cpu_line):
+    import torch
+
+    from rkstiff_gb300 import models, sharding
+    from rkstiff_gb300.ensemble import Ensemble
+    from rkstiff_gb300.solveras import SolverConfig
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    seed = WORKLOAD["seed"] if world == 1 else sharding.weak_seed(WORKLOAD["seed"], rank)
+    inst = make_instances(WORKLOAD["instances"], seed)
+    lins, nls, u0s = [], [], []
+    for n, L, u0 in inst:
+        kx, lin = ks_operator(n, L)
+        lins.append(lin)
+        nls.append(models.ks_ops(kx)[1])
+        u0s.append(u0)
+    ens = Ensemble("ETD35", lins, nls, config=SolverConfig(epsilon=WORKLOAD["epsilon"]), precision="fp32",
+                   device=dev)
+    eng = ens.engine
+    u0_dev = ens.pack(u0s)
+    u = torch.empty_like(u0_dev)
+    tf = WORKLOAD["tf"]
+
+    def one_step():
+        u.copy_(u0_dev)
+        return ens.evolve_packed(u, 0.0, tf)
+
+    for _ in range(args.warmup):
+        st = one_step()
+    torch.cuda.synchronize()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    eng.events = []
+    eng.record_events = True
+    launches0 = eng.launches
+    mode_steps = 0
+    flops = 0.0
+    stream = torch.cuda.current_stream(dev)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        st = one_step()
+        mode_steps += int(np.sum(eng.ms * st["steps"]))
+        flops += flops_of(eng, st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    eng.record_events = False
+    elapsed = e0.elapsed_time(e1) * 1e-3
+    kernel_s = sum(a.elapsed_time(b) for a, b in eng.events) * 1e-3
+    n_launch = eng.launches - launches0
+    status = st["status"]
+    max_elapsed = sharding.max_over_ranks(elapsed, dev)
+    total_mode_steps = sharding.sum_over_ranks(mode_steps, dev)
+    value = total_mode_steps / max_elapsed
+
+    # end to end through the public API with host buffers: pinned host ICs in, finals out
+    host_in = torch.empty(u0_dev.shape, dtype=u0_dev.dtype, pin_memory=True)
+    host_in.copy_(u0_dev.cpu())
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_mode_steps = 0
+    for _ in range(args.steps):
+        u.copy_(host_in, non_blocking=True)
+        st2 = ens.evolve_packed(u, 0.0, tf)
+        host_out.copy_(u, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_mode_steps += int(np.sum(eng.ms * st2["steps"]))
+    e2e_elapsed = sharding.max_over_ranks(time.perf_counter() - t0, dev)
+    e2e_value = sharding.sum_over_ranks(e2e_mode_steps, dev) / e2e_elapsed
+    state_bytes = eng.state_dev.numel()
+    vec_bytes = u.numel() * u.element_size()
+
+    if rank != 0:
+        return
+    peak = measure_fp32_peak(dev)
+    achieved = flops / kernel_s / 1e12
+    counts = {name: int(np.sum(status == code)) for name, code in (("done", 0), ("max_loops", 1), ("min_step", 2))}
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": max_elapsed / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 (complex64 stages/FFTs; FP64 coefficients, error norm, time)",
+        "data": "synthetic (seeded KS ensemble)",
+        "config": {
+            **{k: WORKLOAD[k] for k in ("workload", "instances", "n_choices", "L_range", "epsilon", "tf", "method")},
+            "precision": "fp32",
+            "parallelism": f"instances per GPU, {world} GPU(s)",
+            "l2_flush": "not needed: per-step working set (%d MB scratch + states) exceeds the 126 MB L2"
+                        % (eng.slab_bytes // (1 << 20)),
+            "instance_status": counts,
+        },
+        "roofline": {
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / peak,
+            "traffic": None,
+            "peak_source": "measured in this run by rk_probe_fp32 (FP32 FMA throughput; "
+                           "MEASURED_PEAKS.json carries no FP32 CUDA-core figure)",
+            "flops_per_launch": flops / max(n_launch, 1),
+            "kernel_ms_per_launch": kernel_s / max(n_launch, 1) * 1e3,
+        },
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": vec_bytes + state_bytes,
+                "d2h_bytes_per_step": vec_bytes + state_bytes},
+        "gpu_launches": n_launch,
+        "cpu_baseline": cpu_line,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    cores = host_cores()
+    per_step = max(cores, 2 * cores)
+    inst = make_instances(WORKLOAD["instances"], WORKLOAD["seed"])
+    pool = cpu_pool(cores)
+    try:
+        step = 0
+        for _ in range(args.warmup):
+            sample = inst[(step * per_step) % len(inst):][:per_step]
+            cpu_measure(pool, sample)
+            step += 1
+        total_ms, total_wall = 0, 0.0
+        for _ in range(args.steps):
+            sample = inst[(step * per_step) % len(inst):][:per_step]
+            _, wall, res = cpu_measure(pool, sample)
+            total_ms += sum(m * s for m, s, _, _ in res)
+            total_wall += wall
+            step += 1
+    finally:
+        pool.close()
+        pool.join()
+    value = total_ms / total_wall
+    sample_desc = (f"{per_step} instances per step (of the {WORKLOAD['instances']}), each run to tf=100 by the "
+                   f"NumPy FP64 oracle, one instance per worker, {cores} workers ({cpu_model()})")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_wall / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp64",
+        "data": "synthetic (seeded KS ensemble)",
+        "config": {k: WORKLOAD[k] for k in ("workload", "instances", "n_choices", "L_range", "epsilon", "tf", "method")},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample_desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_line(cores: int):
+    inst = make_instances(WORKLOAD["instances"], WORKLOAD["seed"])
+    sample = inst[: 4 * cores]
+    pool = cpu_pool(cores)
+    try:
+        value, wall, res = cpu_measure(pool, sample)
+    finally:
+        pool.close()
+        pool.join()
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {len(sample)} instances of the workload to tf=100 by the NumPy FP64 oracle, "
+                      f"{cores} worker processes ({cpu_model()}), {wall:.1f} s wall"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank = int(os.environ.get("RANK", 0))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    # the CPU baseline pool is spawned before any CUDA call
+    cpu_line = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_line = cpu_baseline_line(host_cores())
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    gpu_arm(args, rank, world, cpu_line)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,12 @@ int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m
  * (_update_stages) with the built-in nonlinearity fused between in-shared-memory FFTs. */
 int rk_evolve(const rk_batch* b, void* stream);
 
+/* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
+ * each run 8 independent FP32 FMA chains of `iters` steps and write one float to
+ * out[blocks*threads] [device].  FLOPs = 16 * blocks * threads * iters; timing it gives the
+ * FP32 CUDA-core peak the spectral kernels are measured against. */
+int rk_probe_fp32(float* out, int32_t blocks, int32_t threads, int32_t iters, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,22 @@ __global__ void twiddle_kernel(cx<double>* tw64, cx<float>* tw32) {
   if (tw32) tw32[k] = cx<float>{(float)c, (float)(-s)};
 }
 
+// Eight independent FMA chains per thread: sustained FP32 CUDA-core throughput.
+__global__ void fp32_probe_kernel(float* out, int iters) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = (threadIdx.x + k) * 1e-7f;
+  const float b = 0.9999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 static int check_method(int method) {
   if (method < RK_IF34 || method > RK_IF4) {
     set_error("unknown method id " + std::to_string(method));
@@ -86,6 +102,15 @@ int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m
     case RK_IF4: return launch_coeffs_IF4(precision, coef_complex, m, lin_op, h, *etd, out, s);
   }
   return RK_E_ARG;
+}
+
+int rk_probe_fp32(float* out, int32_t blocks, int32_t threads, int32_t iters, void* stream) {
+  if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) {
+    set_error("rk_probe_fp32: invalid argument");
+    return RK_E_ARG;
+  }
+  fp32_probe_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters);
+  return cuda_check(cudaGetLastError(), "fp32 probe launch");
 }
 
 int rk_evolve(const rk_batch* b, void* stream) {

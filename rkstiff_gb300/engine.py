@@ -158,6 +158,9 @@ class DiagEnsemble:
         self.tw = twiddles(dev, self.prec)
         self.cdtype = complex_dtype(self.prec)
         self.set_config(config, etd_config)
+        self.launches = 0          # rk_evolve launches issued by this ensemble
+        self.record_events = False  # when True, (start, end) CUDA events bracket each launch
+        self.events = []
 
     # -- configuration ----------------------------------------------------------------
     def set_config(self, config=None, etd_config=None):
@@ -243,7 +246,16 @@ class DiagEnsemble:
         b.ctl = self.ctl
         b.etd = self.etd
         with torch.cuda.device(self.device):
-            nat.check(self.lib.rk_evolve(ctypes.byref(b), stream_handle(self.device)), "rk_evolve")
+            stream = torch.cuda.current_stream(self.device)
+            if self.record_events:
+                ev0 = torch.cuda.Event(enable_timing=True)
+                ev1 = torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+            nat.check(self.lib.rk_evolve(ctypes.byref(b), stream.cuda_stream), "rk_evolve")
+            if self.record_events:
+                ev1.record(stream)
+                self.events.append((ev0, ev1))
+        self.launches += 1
 
     def evolve(self, u_dev: torch.Tensor, t0, tf, h, store_freq: int = 0, snap_cap: int = 0,
                max_steps: int = 200_000, max_launches: int = 100_000, on_snapshots=None) -> np.ndarray:
