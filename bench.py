@@ -235,6 +235,7 @@ def gpu_arm(args, rank, world, cpu_line):
     ens = Ensemble("ETD35", lins, nls, config=SolverConfig(epsilon=WORKLOAD["epsilon"]), precision="fp32",
                    device=dev)
     eng = ens.engine
+    tuned = ens.autotune(u0s, span=2.0)
     u0_dev = ens.pack(u0s)
     u = torch.empty_like(u0_dev)
     tf = WORKLOAD["tf"]
@@ -325,6 +326,9 @@ def gpu_arm(args, rank, world, cpu_line):
             "l2_flush": "not needed: per-step working set (%d MB scratch + states) exceeds the 126 MB L2"
                         % (eng.slab_bytes // (1 << 20)),
             "instance_status": counts,
+            "launch_shapes": {str(n): "%d threads, %s" % (v["threads"], {-1: "auto", 0: "global", 1: "smem-state",
+                                                                          2: "smem-all"}[v["place"]])
+                              for n, v in tuned.items()},
         },
         "roofline": {
             "bound": "fp32",

@@ -130,10 +130,28 @@ typedef struct rk_batch {
   double* snap_t;          /* [device] snap_cap times per instance                     */
   int64_t max_steps;       /* accepted steps per instance per launch (safety bound)    */
   int32_t run_mode;        /* RK_RUN_EVOLVE / RK_RUN_STEP                              */
-  int32_t threads;         /* threads per instance group, a multiple of 32 <= 256 (0: 256) */
+  int32_t threads;         /* threads per instance group, a multiple of 32 <= 256 (0: auto) */
   rk_controller ctl;
   rk_etd_config etd;
+  /* Optional split of `order` into classes of equal grid size, each launched as its own
+   * kernel on a stream forked from `stream` (joined before rk_evolve returns to the
+   * stream's order), sized for its n.  n_classes = 0: one launch over all instances,
+   * and `queue` needs one counter; otherwise n_classes counters. */
+  int32_t n_classes;
+  int32_t placement;            /* RK_PLACE_* for every class (RK_PLACE_AUTO: per class)  */
+  const int32_t* class_n;       /* [host] grid size of each class                         */
+  const int64_t* class_start;   /* [host] n_classes+1 offsets into `order`                */
+  const int32_t* class_threads; /* [host] threads per instance per class (NULL: auto)     */
+  const int32_t* class_place;   /* [host] placement per class (NULL: `placement`)         */
 } rk_batch;
+
+/* where an instance's scratch arrays live during a launch */
+enum {
+  RK_PLACE_AUTO = -1,
+  RK_PLACE_GLOBAL = 0,     /* all arrays in the global scratch slab                       */
+  RK_PLACE_SMEM_STATE = 1, /* u, unew and stage arrays in shared memory, coefficients global */
+  RK_PLACE_SMEM_ALL = 2    /* all arrays in shared memory (coefficients rebuilt per launch) */
+};
 
 /* ABI version and last error message (thread-local). */
 int rk_abi_version(void);

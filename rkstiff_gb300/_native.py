@@ -24,6 +24,7 @@ RK_RUN_EVOLVE, RK_RUN_STEP = 0, 1
 RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
 RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE = 4, 5, 6
 RK_TW_N = 8192
+RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL = -1, 0, 1, 2
 
 # number of stage arrays and coefficient arrays per method (mirrors rk_evolve.cuh Traits)
 STAGE_ARRAYS = {RK_ETD35: 6, RK_ETD5: 6, RK_ETD34: 5, RK_ETD4: 4, RK_IF34: 5, RK_IF4: 4, RK_IF45DP: 7}
@@ -50,6 +51,9 @@ class RkBatch(ctypes.Structure):
         ("snap_u", ctypes.c_void_p), ("snap_t", ctypes.c_void_p), ("max_steps", ctypes.c_int64),
         ("run_mode", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("ctl", RkController), ("etd", RkEtdConfig),
+        ("n_classes", ctypes.c_int32), ("placement", ctypes.c_int32),
+        ("class_n", ctypes.c_void_p), ("class_start", ctypes.c_void_p),
+        ("class_threads", ctypes.c_void_p), ("class_place", ctypes.c_void_p),
     ]
 
 

@@ -2,7 +2,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "rk_coeffs.cuh"
 #include "rk_evolve.cuh"
@@ -44,6 +46,96 @@ __global__ void fp32_probe_kernel(float* out, int iters) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) s += a[k];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// ---- side streams and events used to fork per-class launches -------------------------
+struct DevicePool {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;
+};
+static std::mutex g_pool_mu;
+static std::vector<DevicePool> g_pools;
+
+static int pool_get(int dev, int need, DevicePool** out) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if ((int)g_pools.size() <= dev) g_pools.resize(dev + 1);
+  DevicePool& p = g_pools[dev];
+  while ((int)p.streams.size() < need) {
+    cudaStream_t s;
+    if (int e = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream")) return e;
+    p.streams.push_back(s);
+  }
+  while ((int)p.events.size() < need + 1) {
+    cudaEvent_t ev;
+    if (int e = cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "fork event")) return e;
+    p.events.push_back(ev);
+  }
+  *out = &p;
+  return RK_OK;
+}
+
+static size_t smem_bytes_method(const rk_batch& b, int n, int place) {
+  switch (b.method) {
+    case RK_IF34: return smem_bytes_IF34(b, n, place);
+    case RK_ETD35: return smem_bytes_ETD35(b, n, place);
+    case RK_ETD34: return smem_bytes_ETD34(b, n, place);
+    case RK_IF45DP: return smem_bytes_IF45DP(b, n, place);
+    case RK_ETD4: return smem_bytes_ETD4(b, n, place);
+    case RK_ETD5: return smem_bytes_ETD5(b, n, place);
+    case RK_IF4: return smem_bytes_IF4(b, n, place);
+  }
+  return 0;
+}
+
+static size_t max_smem_per_block() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
+    v = 227 * 1024;
+  return (size_t)v;
+}
+
+// Placement for a class of grid size n: prefer shared-memory arrays that still leave room
+// for two blocks per SM, then any that fits one block, then the global slab.
+// A single-step run keeps the coefficients in the global slab (they persist between
+// calls); an evolve may rebuild them in shared memory once per launch.
+static int auto_place(const rk_batch& b, int n) {
+  const size_t lim1 = max_smem_per_block();
+  const size_t lim2 = lim1 / 2 - 1024;
+  const bool step = b.run_mode == RK_RUN_STEP;
+  for (size_t lim : {lim2, lim1}) {
+    if (!step && smem_bytes_method(b, n, RK_PLACE_SMEM_ALL) <= lim) return RK_PLACE_SMEM_ALL;
+    if (smem_bytes_method(b, n, RK_PLACE_SMEM_STATE) <= lim) return RK_PLACE_SMEM_STATE;
+  }
+  return RK_PLACE_GLOBAL;
+}
+
+static int auto_threads(int n) {
+  int t = n / 8;
+  if (t < 64) t = 64;
+  if (t > 256) t = 256;
+  return t;
+}
+
+static int launch_class(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
+  if (smem_bytes_method(b, c.n > 0 ? c.n : b.n_max, c.place) > max_smem_per_block()) {
+    set_error("rk_evolve: placement " + std::to_string(c.place) + " needs more shared memory than a block has");
+    return RK_E_SIZE;
+  }
+  if (b.method == RK_ETD35 && c.n > 0) {
+    int e = launch_evolve_etd35_ct(b, c, s);
+    if (e != RK_E_UNSUPPORTED) return e;
+  }
+  switch (b.method) {
+    case RK_IF34: return launch_evolve_IF34(b, c, s);
+    case RK_ETD35: return launch_evolve_ETD35(b, c, s);
+    case RK_ETD34: return launch_evolve_ETD34(b, c, s);
+    case RK_IF45DP: return launch_evolve_IF45DP(b, c, s);
+    case RK_ETD4: return launch_evolve_ETD4(b, c, s);
+    case RK_ETD5: return launch_evolve_ETD5(b, c, s);
+    case RK_IF4: return launch_evolve_IF4(b, c, s);
+  }
+  return RK_E_ARG;
 }
 
 static int check_method(int method) {
@@ -151,22 +243,64 @@ int rk_evolve(const rk_batch* b, void* stream) {
     set_error("rk_evolve: contour_points must be > 1");
     return RK_E_ARG;
   }
-  const int thr = b->threads > 0 ? b->threads : 256;
-  if (thr % 32 || thr > 256) {
-    set_error("rk_evolve: threads must be a multiple of 32 and <= 256");
+  if (b->threads < 0 || b->threads % 32 || b->threads > 256) {
+    set_error("rk_evolve: threads must be 0 (auto) or a multiple of 32 <= 256");
+    return RK_E_ARG;
+  }
+  if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_ALL) {
+    set_error("rk_evolve: unknown placement");
     return RK_E_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  switch (b->method) {
-    case RK_IF34: return launch_evolve_IF34(*b, s);
-    case RK_ETD35: return launch_evolve_ETD35(*b, s);
-    case RK_ETD34: return launch_evolve_ETD34(*b, s);
-    case RK_IF45DP: return launch_evolve_IF45DP(*b, s);
-    case RK_ETD4: return launch_evolve_ETD4(*b, s);
-    case RK_ETD5: return launch_evolve_ETD5(*b, s);
-    case RK_IF4: return launch_evolve_IF4(*b, s);
+  if (b->n_classes <= 0) {
+    ClassLaunch c{b->order, b->n_inst, 0, b->queue, b->threads > 0 ? b->threads : auto_threads(nmax),
+                  b->placement == RK_PLACE_AUTO ? auto_place(*b, nmax) : b->placement};
+    return launch_class(*b, c, s);
   }
-  return RK_E_ARG;
+  if (!b->class_n || !b->class_start) {
+    set_error("rk_evolve: classes requested without class_n / class_start");
+    return RK_E_ARG;
+  }
+  if (b->class_start[0] != 0 || b->class_start[b->n_classes] != b->n_inst) {
+    set_error("rk_evolve: class_start must run from 0 to n_inst");
+    return RK_E_ARG;
+  }
+  std::vector<ClassLaunch> cls;
+  for (int c = 0; c < b->n_classes; ++c) {
+    const int n = b->class_n[c];
+    const int64_t cnt = b->class_start[c + 1] - b->class_start[c];
+    if (n < 4 || (n & (n - 1)) || n > nmax || cnt < 0) {
+      set_error("rk_evolve: class grid sizes must be powers of two <= n_max");
+      return RK_E_SIZE;
+    }
+    int thr = b->class_threads ? b->class_threads[c] : (b->threads > 0 ? b->threads : auto_threads(n));
+    if (thr <= 0 || thr % 32 || thr > 256) {
+      set_error("rk_evolve: class thread counts must be multiples of 32 <= 256");
+      return RK_E_ARG;
+    }
+    int pl = b->class_place ? b->class_place[c] : b->placement;
+    if (pl == RK_PLACE_AUTO) pl = auto_place(*b, n);
+    if (pl < RK_PLACE_GLOBAL || pl > RK_PLACE_SMEM_ALL) {
+      set_error("rk_evolve: unknown class placement");
+      return RK_E_ARG;
+    }
+    if (cnt > 0) cls.push_back(ClassLaunch{b->order + b->class_start[c], cnt, n, b->queue + c, thr, pl});
+  }
+  if (cls.size() == 1) return launch_class(*b, cls[0], s);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  DevicePool* pool = nullptr;
+  if (int e = pool_get(dev, (int)cls.size(), &pool)) return e;
+  if (int e = cuda_check(cudaEventRecord(pool->events[0], s), "fork record")) return e;
+  for (size_t c = 0; c < cls.size(); ++c) {
+    cudaStream_t sc = pool->streams[c];
+    if (int e = cuda_check(cudaStreamWaitEvent(sc, pool->events[0], 0), "fork wait")) return e;
+    if (int e = launch_class(*b, cls[c], sc)) return e;
+    if (int e = cuda_check(cudaEventRecord(pool->events[c + 1], sc), "join record")) return e;
+  }
+  for (size_t c = 0; c < cls.size(); ++c)
+    if (int e = cuda_check(cudaStreamWaitEvent(s, pool->events[c + 1], 0), "join wait")) return e;
+  return RK_OK;
 }
 
 }  // extern "C"

@@ -163,12 +163,113 @@ RK_DEV S direct_hpsi(S z, double h, int order, double num, double den) {
   return h * p;
 }
 
-// psi_order(num/den * (z + r_q)) at one contour node q (the summand of the mean)
-RK_DEV cx<double> contour_term(cx<double> z, const EtdCfg& c, int q, int order, double num, double den) {
-  cx<double> Z = z + contour_node(c, q);
+// psi_order(num/den * Z) at one contour point Z = z + r_q (the summand of the mean)
+RK_DEV cx<double> contour_term_at(cx<double> Z, int order, double num, double den) {
   cx<double> arg = (num == 1.0 && den == 1.0) ? Z : rdiv(num * Z, den);
   cx<double> e = cexp(arg);
   return order == 1 ? psi1(arg, e) : (order == 2 ? psi2(arg, e) : psi3(arg, e));
+}
+
+// complex reciprocal 1/a (Smith's algorithm)
+RK_DEV cx<double> crecip(cx<double> a) { return cdiv(cx<double>{1.0, 0.0}, a); }
+
+// Adds the psi summands of every slot at contour point Z to acc[] with one complex exp
+// (e^{Z/4}; the other scales by products) and one reciprocal per scale (coefficients
+// stored in FP32).
+RK_DEV void contour_terms_fast(int method, cx<double> Z, cx<double>* acc) {
+  auto add = [&](cx<double> x, cx<double> e, cx<double>* out, bool third) {
+    const cx<double> r = crecip(x);
+    const cx<double> em1 = cx<double>{e.x - 1.0, e.y};
+    const cx<double> d = em1 - x;
+    const cx<double> r2 = r * r;
+    out[0] = out[0] + em1 * r;
+    out[1] = out[1] + (2.0 * d) * r2;
+    if (third) out[2] = out[2] + (6.0 * (d - 0.5 * (x * x))) * (r2 * r);
+  };
+  const cx<double> e1 = cexp(0.25 * Z);
+  const cx<double> e2 = e1 * e1;
+  if (method == RK_ETD35 || method == RK_ETD5) {
+    add(0.25 * Z, e1, acc + 0, false);
+    add(0.5 * Z, e2, acc + 2, false);
+    add(0.25 * (3.0 * Z), e2 * e1, acc + 4, false);
+    add(Z, e2 * e2, acc + 6, true);
+  } else {
+    add(0.5 * Z, e2, acc + 0, false);
+    add(Z, e2 * e2, acc + 2, true);
+  }
+}
+
+// Same coefficients with the exponentials E = {e^{z/4}, e^{z/2}, e^{3z/4}, e^z} given
+// (ETD34 uses E[1], E[3]).
+template <class S>
+RK_DEV void etd_from_psi_e(int method, const S* E, const S* P, S* o) {
+  if (method == RK_ETD35 || method == RK_ETD5) {
+    const S p1_14 = P[0], p2_14 = P[1], p1_12 = P[2], p2_12 = P[3], p1_34 = P[4], p2_34 = P[5];
+    const S p1 = P[6], p2 = P[7], p3 = P[8];
+    o[C35_E14] = E[0];
+    o[C35_E12] = E[1];
+    o[C35_E34] = E[2];
+    o[C35_E] = E[3];
+    o[C35_A21] = rdiv(p1_14, 4.0);
+    o[C35_A31] = rdiv(p1_14 - rdiv(p2_14, 2.0), 4.0);
+    o[C35_A32] = rdiv(p2_14, 8.0);
+    o[C35_A41] = rdiv(p1_12 - p2_12, 2.0);
+    o[C35_A43] = rdiv(p2_12, 2.0);
+    o[C35_A51] = rdiv(3.0 * (p1_34 - rdiv(3.0 * p2_34, 4.0)), 4.0);
+    o[C35_A52] = rdiv(-3.0 * p1_34, 8.0);
+    o[C35_A54] = rdiv(9.0 * p2_34, 16.0);
+    o[C35_A61] = rdiv(-77.0 * p1 + 59.0 * p2, 42.0);
+    o[C35_A62] = rdiv(8.0 * p1, 7.0);
+    o[C35_A63] = rdiv(111.0 * p1 - 87.0 * p2, 28.0);
+    o[C35_A65] = rdiv(-47.0 * p1 + 143.0 * p2, 84.0);
+    o[C35_A71] = rdiv(7.0 * ((257.0 * p1 - 497.0 * p2) + 270.0 * p3), 2700.0);
+    o[C35_A73] = rdiv((1097.0 * p1 - 467.0 * p2) - 150.0 * p3, 1350.0);
+    o[C35_A74] = rdiv(2.0 * ((-49.0 * p1 + 199.0 * p2) - 135.0 * p3), 225.0);
+    o[C35_A75] = rdiv((-313.0 * p1 + 883.0 * p2) - 90.0 * p3, 1350.0);
+    o[C35_A76] = rdiv((509.0 * p1 - 2129.0 * p2) + 1830.0 * p3, 2700.0);
+  } else {
+    const S p1_12 = P[0], p2_12 = P[1], p1 = P[2], p2 = P[3], p3 = P[4];
+    o[C34_E] = E[3];
+    o[C34_E2] = E[1];
+    o[C34_A21] = 0.5 * p1_12;
+    o[C34_A31] = 0.5 * (p1_12 - p2_12);
+    o[C34_A32] = 0.5 * p2_12;
+    o[C34_A41] = p1 - p2;
+    o[C34_A43] = p2;
+    o[C34_A51] = (p1 - 1.5 * p2) + (2.0 / 3) * p3;
+    o[C34_A52] = p2 - (2.0 / 3) * p3;
+    o[C34_A54] = -0.5 * p2 + (2.0 / 3) * p3;
+  }
+}
+
+// Reduced-cost FP64 psi set of a real mode for coefficients stored in FP32: one exp
+// (e^{z/4}; the other scales by products) and one reciprocal of z shared by every psi.
+// The results differ from the per-scale formulas by a few FP64 ulps, far below FP32
+// resolution.  E receives {e^{z/4}, e^{z/2}, e^{3z/4}, e^z}.
+RK_DEV void fast_real_psi(int method, double z, double h, double* E, double* P) {
+  const double e1 = exp(0.25 * z);
+  const double e2 = e1 * e1;
+  E[0] = e1;
+  E[1] = e2;
+  E[2] = e2 * e1;
+  E[3] = e2 * e2;
+  const double rz = 1.0 / z;
+  auto psis = [&](double x, double e, double r, double* out, bool third) {
+    const double em1 = e - 1.0;
+    const double d = em1 - x;
+    out[0] = h * (em1 * r);
+    out[1] = h * ((2.0 * d) * (r * r));
+    if (third) out[2] = h * ((6.0 * (d - 0.5 * (x * x))) * (r * (r * r)));
+  };
+  if (method == RK_ETD35 || method == RK_ETD5) {
+    psis(0.25 * z, E[0], 4.0 * rz, P + 0, false);
+    psis(0.5 * z, E[1], 2.0 * rz, P + 2, false);
+    psis(0.25 * (3.0 * z), E[2], rz * (4.0 / 3.0), P + 4, false);
+    psis(z, E[3], rz, P + 6, true);
+  } else {
+    psis(0.5 * z, E[1], 2.0 * rz, P + 0, false);
+    psis(z, E[3], rz, P + 2, true);
+  }
 }
 
 template <class S>

@@ -49,7 +49,9 @@ RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m)
 // ---------------------------------------------------------------------------------
 // per-instance working context
 // ---------------------------------------------------------------------------------
-template <class T, class CT>
+// LOGN > 0: the grid size is the compile-time constant 2^LOGN (register-radix FFTs);
+// LOGN == 0: runtime size (radix-4 FFTs).
+template <class T, class CT, int LOGN = 0>
 struct Ctx {
   Group g;
   int n, logn, m, mp, nl_kind;
@@ -70,14 +72,16 @@ struct Ctx {
 // ---------------------------------------------------------------------------------
 // built-in nonlinearities: out[j] = N(k)[j] with k[j] = kf(j)
 // ---------------------------------------------------------------------------------
-template <class T, class CT, class KF>
-RK_DEV void nl_eval(const Ctx<T, CT>& x, KF kf, cx<T>* __restrict__ out) {
+template <class T, class CT, int LOGN, class KF>
+RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
   const Group& g = x.g;
+  // FFT-buffer index: padded for the compile-time transforms
+  auto P = [](int c) { return LOGN > 0 ? fpad(c) : c; };
   if (x.nl_kind == RK_NL_UUX) {
     // u = irfft(k), ux = irfft(i kx k) packed as one complex inverse FFT of length n:
     // Z = A + iB with A, B the Hermitian spectra; numpy's irfft drops the imaginary
     // parts of the DC and Nyquist bins, so they are dropped here too.
-    const int n = x.n, M = n >> 1;
+    const int n = LOGN > 0 ? (1 << LOGN) : x.n, M = n >> 1;
     const T inv_n = T(1) / T(n);
     cx<T>* Z = x.fa;
     for (int j = g.tid; j <= M; j += g.nthr) {
@@ -88,24 +92,35 @@ RK_DEV void nl_eval(const Ctx<T, CT>& x, KF kf, cx<T>* __restrict__ out) {
         A.y = T(0);
         B.y = T(0);
       }
-      Z[j] = cx<T>{A.x - B.y, A.y + B.x};
-      if (j > 0 && j < M) Z[n - j] = cx<T>{A.x + B.y, B.x - A.y};
+      Z[P(j)] = cx<T>{A.x - B.y, A.y + B.x};
+      if (j > 0 && j < M) Z[P(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
     }
     g.sync();
-    cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
-    cx<T>* other = (z == x.fa) ? x.fb : x.fa;
-    T* w = reinterpret_cast<T*>(other);
-    for (int t = g.tid; t < n; t += g.nthr) {
-      cx<T> v = z[t];
-      w[t] = v.x * v.y;
+    cx<T>* F;
+    if constexpr (LOGN > 0) {
+      // last inverse pass writes the real product u*ux; the forward transform of
+      // length n/2 reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
+      cx<T>* w = fft_ct<T, LOGN, true>(g, x.fa, x.fb, x.tw, [](cx<T>* y, int idx, cx<T> v) {
+        reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
+      });
+      cx<T>* other = (w == x.fa) ? x.fb : x.fa;
+      F = fft_ct<T, LOGN - 1, false>(g, w, other, x.tw, StoreY<T>());
+    } else {
+      cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
+      cx<T>* other = (z == x.fa) ? x.fb : x.fa;
+      T* w = reinterpret_cast<T*>(other);
+      for (int t = g.tid; t < n; t += g.nthr) {
+        cx<T> v = z[t];
+        w[t] = v.x * v.y;
+      }
+      g.sync();
+      F = fft_group<T, false>(g, other, z, x.logn - 1, x.tw);
     }
-    g.sync();
-    // rfft of the real product via a complex FFT of length n/2 and the split formula
-    cx<T>* F = fft_group<T, false>(g, other, z, x.logn - 1, x.tw);
-    const int tws = RK_TW_N >> x.logn;
+    // rfft of the real product from the length-n/2 transform (split formula)
+    const int tws = LOGN > 0 ? (RK_TW_N >> LOGN) : (RK_TW_N >> x.logn);
     for (int k = g.tid; k <= M; k += g.nthr) {
-      cx<T> Fk = F[k == M ? 0 : k];
-      cx<T> Fm = conj(F[k == 0 ? 0 : M - k]);
+      cx<T> Fk = F[P(k == M ? 0 : k)];
+      cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
       cx<T> Fe = (Fk + Fm) * T(0.5);
       cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
       cx<T> W = Fe + x.tw[k * tws] * Fo;
@@ -114,21 +129,31 @@ RK_DEV void nl_eval(const Ctx<T, CT>& x, KF kf, cx<T>* __restrict__ out) {
     g.sync();
   } else if (x.nl_kind == RK_NL_NLS) {
     // v = ifft(k); N = fft(i c |v|^2 v)
-    const int n = x.n;
+    const int n = LOGN > 0 ? (1 << LOGN) : x.n;
     const T inv_n = T(1) / T(n);
-    for (int j = g.tid; j < n; j += g.nthr) x.fa[j] = kf(j) * inv_n;
+    for (int j = g.tid; j < n; j += g.nthr) x.fa[P(j)] = kf(j) * inv_n;
     g.sync();
-    cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
-    cx<T>* other = (z == x.fa) ? x.fb : x.fa;
-    for (int t = g.tid; t < n; t += g.nthr) {
-      cx<T> v = z[t];
-      T a2 = (v.x * v.x + v.y * v.y) * x.nl_c;
-      other[t] = cx<T>{-a2 * v.y, a2 * v.x};
+    const T c = x.nl_c;
+    if constexpr (LOGN > 0) {
+      cx<T>* w = fft_ct<T, LOGN, true>(g, x.fa, x.fb, x.tw, [c](cx<T>* y, int idx, cx<T> v) {
+        T a2 = (v.x * v.x + v.y * v.y) * c;
+        y[fpad(idx)] = cx<T>{-a2 * v.y, a2 * v.x};
+      });
+      cx<T>* other = (w == x.fa) ? x.fb : x.fa;
+      fft_ct<T, LOGN, false>(g, w, other, x.tw, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
+    } else {
+      cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
+      cx<T>* other = (z == x.fa) ? x.fb : x.fa;
+      for (int t = g.tid; t < n; t += g.nthr) {
+        cx<T> v = z[t];
+        T a2 = (v.x * v.x + v.y * v.y) * c;
+        other[t] = cx<T>{-a2 * v.y, a2 * v.x};
+      }
+      g.sync();
+      cx<T>* F = fft_group<T, false>(g, other, z, x.logn, x.tw);
+      for (int k = g.tid; k < n; k += g.nthr) out[k] = F[k];
+      g.sync();
     }
-    g.sync();
-    cx<T>* F = fft_group<T, false>(g, other, z, x.logn, x.tw);
-    for (int k = g.tid; k < n; k += g.nthr) out[k] = F[k];
-    g.sync();
   } else {
     for (int k = g.tid; k < x.m; k += g.nthr) out[k] = cx<T>{T(0), T(0)};
     g.sync();
@@ -148,56 +173,71 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
   return cx<double>{h * L.x, h * L.y};
 }
 
-// S: double for a real operator (CT real), cx<double> for a complex one.
-template <class T, class CT, class S, int METHOD>
-RK_DEV void compute_coeffs(const Ctx<T, CT>& x, double h, const EtdCfg& ec) {
-  const Group& g = x.g;
+// Coefficients of one instance at step h into C (array c at C + c*mp).  S is double for
+// a real operator (CT real) and cx<double> for a complex one.  FAST selects the
+// reduced-cost psi evaluation for real modes (coefficients stored in FP32).  Kept out of
+// line: it runs on a small fraction of attempts and would otherwise inflate the
+// register budget of the stage loop.
+template <class CT, class S, int METHOD, bool FAST>
+__device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const cx<double>* __restrict__ lin,
+                                                 CT* __restrict__ C, double h, EtdCfg ec) {
   constexpr int NC = Traits<METHOD>::NC;
   if (!is_etd(METHOD)) {
-    for (int j = g.tid; j < x.m; j += g.nthr) {
-      S z = load_z<S>(x.lin, j, h);
+    for (int j = g.tid; j < m; j += g.nthr) {
+      S z = load_z<S>(lin, j, h);
       S o[NC];
       if_coeffs<S>(METHOD, z, h, o);
 #pragma unroll
-      for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+      for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
     }
     g.sync();
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
   // pass 1: thread per mode, direct formula for |z| >= modecutoff
-  for (int j = g.tid; j < x.m; j += g.nthr) {
-    S z = load_z<S>(x.lin, j, h);
+  for (int j = g.tid; j < m; j += g.nthr) {
+    S z = load_z<S>(lin, j, h);
     if (sabs(z) < ec.cutoff) continue;
     S P[NP];
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-      int order;
-      double num, den;
-      psi_slot(METHOD, k, order, num, den);
-      P[k] = direct_hpsi(z, h, order, num, den);
-    }
     S o[NC];
-    etd_from_psi<S>(METHOD, z, P, o);
+    if constexpr (FAST && sizeof(S) == sizeof(double)) {
+      double E[4];
+      fast_real_psi(METHOD, sre(z), h, E, reinterpret_cast<double*>(P));
+      etd_from_psi_e<double>(METHOD, E, reinterpret_cast<double*>(P), reinterpret_cast<double*>(o));
+    } else {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+      for (int k = 0; k < NP; ++k) {
+        int order;
+        double num, den;
+        psi_slot(METHOD, k, order, num, den);
+        P[k] = direct_hpsi(z, h, order, num, den);
+      }
+      etd_from_psi<S>(METHOD, z, P, o);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
   }
   // pass 2: warp per small mode, lanes over the contour nodes (rkstiff/etd35.py:257-288)
   const int lane = g.tid & 31, warp = g.tid >> 5, nwarp = g.nthr >> 5;
-  for (int j = warp; j < x.m; j += nwarp) {
-    S z = load_z<S>(x.lin, j, h);
+  for (int j = warp; j < m; j += nwarp) {
+    S z = load_z<S>(lin, j, h);
     if (!(sabs(z) < ec.cutoff)) continue;
     cx<double> zc = to_cx(z);
     cx<double> acc[NP];
 #pragma unroll
     for (int k = 0; k < NP; ++k) acc[k] = cx<double>{0.0, 0.0};
     for (int q = lane; q < ec.np; q += 32) {
+      const cx<double> Z = zc + contour_node(ec, q);
+      if constexpr (FAST) {
+        contour_terms_fast(METHOD, Z, acc);
+      } else {
 #pragma unroll
-      for (int k = 0; k < NP; ++k) {
-        int order;
-        double num, den;
-        psi_slot(METHOD, k, order, num, den);
-        acc[k] = acc[k] + contour_term(zc, ec, q, order, num, den);
+        for (int k = 0; k < NP; ++k) {
+          int order;
+          double num, den;
+          psi_slot(METHOD, k, order, num, den);
+          acc[k] = acc[k] + contour_term_at(Z, order, num, den);
+        }
       }
     }
     S P[NP];
@@ -210,10 +250,15 @@ RK_DEV void compute_coeffs(const Ctx<T, CT>& x, double h, const EtdCfg& ec) {
       S o[NC];
       etd_from_psi<S>(METHOD, z, P, o);
 #pragma unroll
-      for (int c = 0; c < NC; ++c) store_c(x.C[c * x.mp + j], o[c]);
+      for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
     }
   }
   g.sync();
+}
+
+template <class T, class CT, class S, int METHOD, int LOGN>
+RK_DEV void compute_coeffs(const Ctx<T, CT, LOGN>& x, double h, const EtdCfg& ec) {
+  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec);
 }
 
 // ---------------------------------------------------------------------------------
@@ -221,43 +266,86 @@ RK_DEV void compute_coeffs(const Ctx<T, CT>& x, double h, const EtdCfg& ec) {
 // ---------------------------------------------------------------------------------
 template <class T> RK_DEV double cabs_d(cx<T> v) { return hypot((double)v.x, (double)v.y); }
 
-template <class T, class CT, class KF>
-RK_DEV double write_unew(const Ctx<T, CT>& x, KF kf) {
-  double mx = 0.0;
+// New state into unew; returns the group-wide max of |unew| (FP64 working precision)
+// or of |unew|^2 (FP32 working precision), NaN if any entry is NaN.
+template <class T, class CT, int LOGN, class KF>
+RK_DEV double write_unew(const Ctx<T, CT, LOGN>& x, KF kf) {
   bool nan = false;
-  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
-    cx<T> v = kf(j);
-    x.unew[j] = v;
-    double a = cabs_d(v);
-    if (a != a) nan = true;
-    else mx = fmax(mx, a);
+  if constexpr (sizeof(T) == sizeof(double)) {
+    double mx = 0.0;
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+      cx<T> v = kf(j);
+      x.unew[j] = v;
+      double a = cabs_d(v);
+      if (a != a) nan = true;
+      else mx = fmax(mx, a);
+    }
+    return group_max_nan(x.g, x.red, nan ? nan_d() : mx);
+  } else {
+    float mx = 0.f;
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+      cx<T> v = kf(j);
+      x.unew[j] = v;
+      float a2 = v.x * v.x + v.y * v.y;
+      if (a2 != a2) nan = true;
+      else mx = fmaxf(mx, a2);
+    }
+    return group_max_nan(x.g, x.red, nan ? nan_d() : (double)mx);
   }
-  return group_max_nan(x.g, x.red, nan ? nan_d() : mx);
 }
 
-template <class T, class CT, class EF>
-RK_DEV double controller_s(const Ctx<T, CT>& x, double maxu, EF ef, const rk_controller& ctl, int q) {
+// s = safety (eps |unew[mask]| / |err[mask]|)^(1/q), mask = |unew| / max|unew| > cutoff
+// (rkstiff/solveras.py:451-455).  The sums of squares are accumulated in FP64.  In FP32
+// working precision the mask is evaluated on squared magnitudes, |u|^2 > cutoff^2 max|u|^2,
+// which needs no square root or division per mode.
+template <class T, class CT, int LOGN, class EF>
+RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const rk_controller& ctl, int q) {
   double su = 0.0, se = 0.0;
-  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
-    cx<T> v = x.unew[j];
-    double a = cabs_d(v);
-    if (a / maxu > ctl.adapt_cutoff) {
-      su += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-      cx<T> e = ef(j);
-      se += (double)e.x * (double)e.x + (double)e.y * (double)e.y;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+      cx<T> v = x.unew[j];
+      double a = cabs_d(v);
+      if (a / maxu > ctl.adapt_cutoff) {
+        su += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        cx<T> e = ef(j);
+        se += (double)e.x * (double)e.x + (double)e.y * (double)e.y;
+      }
+    }
+  } else {
+    // maxu holds max |unew|^2 here; NaN keeps every comparison false, as in the reference
+    const float thr = (float)(ctl.adapt_cutoff * ctl.adapt_cutoff * maxu);
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+      cx<T> v = x.unew[j];
+      float a2 = v.x * v.x + v.y * v.y;
+      if (a2 > thr) {
+        su += (double)a2;
+        cx<T> e = ef(j);
+        se += (double)(e.x * e.x + e.y * e.y);
+      }
     }
   }
   group_sum2(x.g, x.red, su, se);
-  double tol = ctl.epsilon * sqrt(su);
-  return ctl.safety_f * pow(tol / sqrt(se), 1.0 / q);
+  if constexpr (sizeof(T) == sizeof(double)) {
+    double tol = ctl.epsilon * sqrt(su);
+    return ctl.safety_f * pow(tol / sqrt(se), 1.0 / q);
+  } else {
+    // (eps |u| / |err|)^(1/q) = ratio^(1/(2q)) with ratio = eps^2 su / se formed in FP64;
+    // the fractional power runs in FP32 (FP64 pow is a long dependent chain on this GPU).
+    // Edge values keep the reference's outcome: 0/0 -> NaN and x/0 -> inf (both rejected),
+    // a finite ratio beyond FP32 range stays finite (accepted).
+    double ratio = (ctl.epsilon * ctl.epsilon * su) / se;
+    if (ratio != ratio || isinf(ratio)) return ctl.safety_f * ratio;
+    float rf = (float)fmin(ratio, 1e30);
+    return ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / (float)q));
+  }
 }
 
 // ---------------------------------------------------------------------------------
 // stage programs.  Each computes N2.. and unew (and N(unew) where the method needs it)
 // and returns s (adaptive) or 0 (constant).  N1 must be valid on entry.
 // ---------------------------------------------------------------------------------
-template <class T, class CT>
-RK_DEV double attempt_etd35_family(const Ctx<T, CT>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
+template <class T, class CT, int LOGN>
+RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
   const cx<T>* u = x.u;
   cx<T>* const* N = x.N;
   // rkstiff/etd35.py:320-345 (ETD5: etd5.py:236-260)
@@ -298,8 +386,8 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT>& x, bool adaptive, const rk_
   }, ctl, 4);
 }
 
-template <class T, class CT>
-RK_DEV double attempt_etd34_family(const Ctx<T, CT>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
+template <class T, class CT, int LOGN>
+RK_DEV double attempt_etd34_family(const Ctx<T, CT, LOGN>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
   const cx<T>* u = x.u;
   cx<T>* const* N = x.N;
   // rkstiff/etd34.py:182-190 (ETD4: etd4.py:167-174)
@@ -329,8 +417,8 @@ RK_DEV double attempt_etd34_family(const Ctx<T, CT>& x, bool adaptive, const rk_
   return controller_s(x, mx, [&](int j) { return cmul(x.c(C34_A54, j), N[3][j] - N[4][j]); }, ctl, 4);
 }
 
-template <class T, class CT>
-RK_DEV double attempt_if34_family(const Ctx<T, CT>& x, double hd, bool adaptive, const rk_controller& ctl,
+template <class T, class CT, int LOGN>
+RK_DEV double attempt_if34_family(const Ctx<T, CT, LOGN>& x, double hd, bool adaptive, const rk_controller& ctl,
                                   int& nl_count) {
   const cx<T>* u = x.u;
   cx<T>* const* N = x.N;
@@ -360,8 +448,8 @@ RK_DEV double attempt_if34_family(const Ctx<T, CT>& x, double hd, bool adaptive,
   return controller_s(x, mx, [&](int j) { return (h * (N[3][j] - N[4][j])) * r6; }, ctl, 4);
 }
 
-template <class T, class CT>
-RK_DEV double attempt_if45dp(const Ctx<T, CT>& x, double hd, const rk_controller& ctl, int& nl_count) {
+template <class T, class CT, int LOGN>
+RK_DEV double attempt_if45dp(const Ctx<T, CT, LOGN>& x, double hd, const rk_controller& ctl, int& nl_count) {
   const cx<T>* u = x.u;
   cx<T>* const* N = x.N;
   const T a76 = T(dp_a76(hd)), r6 = T(dp_r6(hd)), r7 = T(dp_r7(hd));
@@ -397,8 +485,8 @@ RK_DEV double attempt_if45dp(const Ctx<T, CT>& x, double hd, const rk_controller
   }, ctl, 5);
 }
 
-template <class T, class CT, int METHOD>
-RK_DEV double run_attempt(const Ctx<T, CT>& x, double h, const rk_controller& ctl, int& nl_count) {
+template <class T, class CT, int METHOD, int LOGN>
+RK_DEV double run_attempt(const Ctx<T, CT, LOGN>& x, double h, const rk_controller& ctl, int& nl_count) {
   switch (METHOD) {
     case RK_ETD35: return attempt_etd35_family(x, true, ctl, nl_count);
     case RK_ETD5: return attempt_etd35_family(x, false, ctl, nl_count);
@@ -427,14 +515,22 @@ RK_DEV double accept_h(double s, double h, const rk_controller& c) {
 
 // ---------------------------------------------------------------------------------
 // one instance, start to pause/finish
+//
+// PLACE selects where the instance's arrays live: PL_GLOBAL (all in the global scratch
+// slab), PL_SMEM_STATE (u, unew and the stage arrays in shared memory, coefficients in
+// the global slab), PL_SMEM_ALL (everything in shared memory; the coefficients are then
+// rebuilt at the start of every launch).
 // ---------------------------------------------------------------------------------
-template <class T, class CT, class S, int METHOD>
-RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red) {
+enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
+
+template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
+RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
+                         unsigned char* sm_slab) {
   using Tr = Traits<METHOD>;
-  Ctx<T, CT> x;
+  Ctx<T, CT, LOGN> x;
   x.g = g;
-  x.n = b.n[inst];
-  x.logn = 31 - __clz(x.n);
+  x.n = LOGN > 0 ? (1 << LOGN) : b.n[inst];
+  x.logn = LOGN > 0 ? LOGN : 31 - __clz(x.n);
   x.nl_kind = b.nl_kind;
   x.m = (b.nl_kind == RK_NL_UUX) ? (x.n / 2 + 1) : x.n;
   x.mp = (int)round_up4(x.m);
@@ -442,11 +538,13 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   const int64_t mo = b.mode_off[inst];
   x.kx = b.kx ? b.kx + mo : nullptr;
   x.lin = reinterpret_cast<const cx<double>*>(b.lin_op) + mo;
-  cx<T>* sl = reinterpret_cast<cx<T>*>(reinterpret_cast<char*>(b.slab) + b.slab_off[inst]);
-  x.u = sl;
-  x.unew = sl + x.mp;
-  for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? sl + (2 + i) * x.mp : nullptr;
-  x.C = reinterpret_cast<CT*>(sl + (2 + Tr::NN) * x.mp);
+  cx<T>* gsl = reinterpret_cast<cx<T>*>(reinterpret_cast<char*>(b.slab) + b.slab_off[inst]);
+  cx<T>* ssl = PLACE == PL_GLOBAL ? gsl : reinterpret_cast<cx<T>*>(sm_slab);
+  x.u = ssl;
+  x.unew = ssl + x.mp;
+  for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + (2 + i) * x.mp : nullptr;
+  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + (2 + Tr::NN) * x.mp)
+                             : reinterpret_cast<CT*>(gsl + (2 + Tr::NN) * x.mp);
   x.fa = fa;
   x.fb = fb;
   x.red = red;
@@ -461,7 +559,8 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   for (int j = g.tid; j < x.m; j += g.nthr) x.u[j] = uio[j];
   g.sync();
 
-  double t = st.t, tf = st.tf, h = st.h, hc = st.h_coeff;
+  double t = st.t, tf = st.tf, h = st.h;
+  double hc = PLACE == PL_SMEM_ALL ? nan_d() : st.h_coeff;
   bool accept = st.accept != 0;
   bool n1_valid = false;
   const bool resumed = st.steps > 0;
@@ -553,7 +652,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   if (g.tid == 0) {
     st.t = t;
     st.h = h;
-    st.h_coeff = hc;
+    st.h_coeff = PLACE == PL_SMEM_ALL ? nan_d() : hc;
     st.h_used = h_used;
     st.h_suggest = h_sug;
     st.s_last = s_last;
@@ -566,48 +665,60 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     st.coeff_updates += coeff_updates;
     b.state[inst] = st;
   }
-  // The swapped u/unew roles mean the slab's first array may no longer hold u; only the
+  // The swapped u/unew roles mean the first state array may no longer hold u; only the
   // copy in `uio` is authoritative between launches, so nothing else is persisted.
   g.sync();
 }
 
-template <class T, class CT, class S, int METHOD>
-__global__ void __launch_bounds__(256, 1) evolve_kernel(const rk_batch b, int nfft) {
+// Shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction scratch,
+// the work-item slot, then (PLACE > 0) the instance arrays for mp_s modes.
+template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
+__global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const int32_t* __restrict__ order,
+                                                        int64_t count, int32_t* queue, int nfft) {
   extern __shared__ __align__(16) unsigned char smem[];
   cx<T>* fa = reinterpret_cast<cx<T>*>(smem);
-  cx<T>* fb = fa + nfft;
-  double* red = reinterpret_cast<double*>(fb + nfft);
+  cx<T>* fb = fa + fpad_size(nfft);
+  double* red = reinterpret_cast<double*>(fb + fpad_size(nfft));
   int* item_s = reinterpret_cast<int*>(red + 64);
+  unsigned char* sm_slab = reinterpret_cast<unsigned char*>(red + 66);
   Group g{(int)threadIdx.x, (int)blockDim.x, 0};
   for (;;) {
-    if (g.tid == 0) *item_s = atomicAdd(b.queue, 1);
+    if (g.tid == 0) *item_s = atomicAdd(queue, 1);
     g.sync();
     const int item = *item_s;
     g.sync();
-    if (item >= b.n_inst) break;
-    const int inst = b.order ? b.order[item] : item;
-    run_instance<T, CT, S, METHOD>(b, inst, g, fa, fb, red);
+    if (item >= count) break;
+    const int inst = order ? order[item] : item;
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab);
   }
 }
 
 template <class T, class CT, class S, int METHOD>
 __global__ void coeff_kernel(int m, const double* lin, double h, rk_etd_config etd, CT* out) {
   // standalone coefficient evaluation for one operator (blocks split the modes)
-  Ctx<T, CT> x;
-  x.g = Group{(int)threadIdx.x, (int)blockDim.x, 0};
+  const Group g{(int)threadIdx.x, (int)blockDim.x, 0};
   const int per = blockDim.x;
   const int j0 = blockIdx.x * per;
-  x.m = min(per, m - j0);
-  x.mp = m;  // arrays of length m, shifted so that c*mp + j addresses mode j0 + j
-  x.lin = reinterpret_cast<const cx<double>*>(lin) + j0;
-  x.C = out + j0;
   const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points};
-  compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+  // arrays of length m, shifted so that c*m + j addresses mode j0 + j
+  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(g, min(per, m - j0), m,
+                                                                reinterpret_cast<const cx<double>*>(lin) + j0,
+                                                                out + j0, h, ec);
 }
 
-// smem bytes of the evolve kernel for complex FFT length nfft
+// bytes of the per-instance arrays held in shared memory under placement `place`
+template <class T, class CT, int METHOD>
+inline size_t smem_slab_bytes(int place, int64_t m) {
+  const size_t mp = (size_t)round_up4(m);
+  size_t bytes = 0;
+  if (place >= PL_SMEM_STATE) bytes += (2 + Traits<METHOD>::NN) * mp * sizeof(cx<T>);
+  if (place >= PL_SMEM_ALL) bytes += Traits<METHOD>::NC * mp * sizeof(CT);
+  return bytes;
+}
+
+// smem bytes of the evolve kernel's FFT buffers and scratch for complex FFT length nfft
 template <class T> inline size_t evolve_smem(int nfft) {
-  return 2 * (size_t)nfft * sizeof(cx<T>) + 64 * sizeof(double) + 16;
+  return 2 * (size_t)fpad_size(nfft) * sizeof(cx<T>) + 66 * sizeof(double);
 }
 
 }  // namespace rk

@@ -83,3 +83,183 @@ RK_DEV cx<T>* fft_group(const Group& g, cx<T>* __restrict__ a, cx<T>* __restrict
 }
 
 }  // namespace rk
+
+namespace rk {
+
+// ---------------------------------------------------------------------------------
+// Compile-time-size FFT: Stockham passes of radix 16/8/4/2 with the butterfly held in
+// registers.  LOGN = sum of the pass radices' log2; one barrier per pass.
+// ---------------------------------------------------------------------------------
+
+// multiply by W_16^e = exp(-+2 pi i e/16) with e a compile-time constant
+template <class T, bool INV, int E>
+RK_DEV cx<T> mul_w16(cx<T> v) {
+  constexpr int e = E & 15;
+  if constexpr (e == 0) return v;
+  else if constexpr (e == 4) return INV ? mul_i(v) : mul_mi(v);
+  else if constexpr (e == 8) return -v;
+  else if constexpr (e == 12) return INV ? mul_mi(v) : mul_i(v);
+  else {
+    // W = cos(2 pi e/16) -/+ i sin(2 pi e/16); sin(2 pi e/16) = cos(2 pi (e - 4)/16)
+    constexpr double c = e == 1 ? 0.9238795325112867 : e == 2 ? 0.7071067811865476 : e == 3 ? 0.3826834323650898
+                       : e == 5 ? -0.3826834323650898 : e == 6 ? -0.7071067811865476 : e == 7 ? -0.9238795325112867
+                       : e == 9 ? -0.9238795325112867 : e == 10 ? -0.7071067811865476 : e == 11 ? -0.3826834323650898
+                       : e == 13 ? 0.3826834323650898 : e == 14 ? 0.7071067811865476 : 0.9238795325112867;
+    constexpr double s = e == 1 ? 0.3826834323650898 : e == 2 ? 0.7071067811865476 : e == 3 ? 0.9238795325112867
+                       : e == 5 ? 0.9238795325112867 : e == 6 ? 0.7071067811865476 : e == 7 ? 0.3826834323650898
+                       : e == 9 ? -0.3826834323650898 : e == 10 ? -0.7071067811865476 : e == 11 ? -0.9238795325112867
+                       : e == 13 ? -0.9238795325112867 : e == 14 ? -0.7071067811865476 : -0.3826834323650898;
+    const T cc = T(c), ss = INV ? T(s) : T(-s);
+    return cx<T>{v.x * cc - v.y * ss, v.x * ss + v.y * cc};
+  }
+}
+
+// Padded shared-memory index of complex element c: one spare slot per 16 elements, so a
+// pass that stores at a stride of 16 elements spreads over the banks.
+RK_HD constexpr int fpad(int c) { return c + (c >> 4); }
+// complex slots a padded buffer of n elements occupies
+RK_HD constexpr int fpad_size(int n) { return n + (n >> 4); }
+
+template <class T, bool INV>
+RK_DEV void dft2(cx<T>& a, cx<T>& b) {
+  cx<T> t = a - b;
+  a = a + b;
+  b = t;
+}
+
+// In-register DFT of size R in natural order: v[k] <- sum_j v[j] W_R^{jk}.
+template <class T, int R, bool INV>
+RK_DEV void dft_reg(cx<T>* v) {
+  if constexpr (R == 2) {
+    dft2<T, INV>(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    dft4<T, INV>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    // 8 = 2 x 4: inner 4-point DFTs over the even/odd halves, twiddle, 2-point combine
+    cx<T> e[4] = {v[0], v[2], v[4], v[6]};
+    cx<T> o[4] = {v[1], v[3], v[5], v[7]};
+    dft4<T, INV>(e[0], e[1], e[2], e[3]);
+    dft4<T, INV>(o[0], o[1], o[2], o[3]);
+    o[1] = mul_w16<T, INV, 2>(o[1]);
+    o[2] = mul_w16<T, INV, 4>(o[2]);
+    o[3] = mul_w16<T, INV, 6>(o[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = e[k] + o[k];
+      v[k + 4] = e[k] - o[k];
+    }
+  } else {
+    static_assert(R == 16, "radix must be 2, 4, 8 or 16");
+    // 16 = 4 x 4: y[k1][n2] = DFT4 over n1 of x[4 n1 + n2]; twiddle W16^{n2 k1};
+    // X[k1 + 4 k2] = DFT4 over n2 of y[k1][n2]
+    cx<T> w[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      cx<T> a0 = v[n2], a1 = v[4 + n2], a2 = v[8 + n2], a3 = v[12 + n2];
+      dft4<T, INV>(a0, a1, a2, a3);
+      w[0 * 4 + n2] = a0;
+      w[1 * 4 + n2] = a1;
+      w[2 * 4 + n2] = a2;
+      w[3 * 4 + n2] = a3;
+    }
+    w[5] = mul_w16<T, INV, 1>(w[5]);
+    w[6] = mul_w16<T, INV, 2>(w[6]);
+    w[7] = mul_w16<T, INV, 3>(w[7]);
+    w[9] = mul_w16<T, INV, 2>(w[9]);
+    w[10] = mul_w16<T, INV, 4>(w[10]);
+    w[11] = mul_w16<T, INV, 6>(w[11]);
+    w[13] = mul_w16<T, INV, 3>(w[13]);
+    w[14] = mul_w16<T, INV, 6>(w[14]);
+    w[15] = mul_w16<T, INV, 9>(w[15]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      cx<T> a0 = w[4 * k1], a1 = w[4 * k1 + 1], a2 = w[4 * k1 + 2], a3 = w[4 * k1 + 3];
+      dft4<T, INV>(a0, a1, a2, a3);
+      v[k1] = a0;
+      v[k1 + 4] = a1;
+      v[k1 + 8] = a2;
+      v[k1 + 12] = a3;
+    }
+  }
+}
+
+// radix of pass p for a size-2^LOGN transform: 16 while >= 4 bits remain... then the rest
+template <int LOGN, int P>
+struct PassRadix {
+  __host__ __device__ static constexpr int used() {
+    int left = LOGN, lg = 0;
+    for (int q = 0; q <= P; ++q) {
+      lg = left >= 4 ? 4 : left;
+      // prefer 8+8 over 16+4 / 16+2 splits of the last 6/5 bits
+      if (left == 6 || left == 5) lg = 3;
+      if (left == 7) lg = 4;
+      left -= lg;
+    }
+    return lg;
+  }
+  __host__ __device__ static constexpr int bits_before() {
+    int left = LOGN, done = 0;
+    for (int q = 0; q < P; ++q) {
+      int lg = left >= 4 ? 4 : left;
+      if (left == 6 || left == 5) lg = 3;
+      if (left == 7) lg = 4;
+      left -= lg;
+      done += lg;
+    }
+    return done;
+  }
+};
+
+// One Stockham pass of radix R = 2^LGR at sub-length Ls = 2^LGLS over N = 2^LOGN points.
+// `post(idx, value)` receives the output (final pass) -- by default a store to y.
+template <class T, int LOGN, int LGR, int LGLS, bool INV, class Store>
+RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ tw, Store store) {
+  constexpr int N = 1 << LOGN, R = 1 << LGR, Ls = 1 << LGLS, NB = N / R;
+  constexpr int TWS = RK_TW_N >> (LGLS + LGR);  // table stride of W_{R Ls}
+  for (int i = g.tid; i < NB; i += g.nthr) {
+    const int k = i & (Ls - 1);
+    cx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = x[fpad(i + r * NB)];
+    if constexpr (Ls > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tw, r * k * TWS);
+    }
+    dft_reg<T, R, INV>(v);
+    const int j = ((i - k) << LGR) + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) store(j + r * Ls, v[r]);
+  }
+}
+
+template <class T, int LOGN, int P, bool INV, class FinalStore>
+RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw, FinalStore fin) {
+  constexpr int LGR = PassRadix<LOGN, P>::used();
+  constexpr int DONE = PassRadix<LOGN, P>::bits_before();
+  if constexpr (DONE + LGR == LOGN) {
+    // final pass: outputs go to fin(y, index, value); y is the buffer not being read
+    stockham_pass<T, LOGN, LGR, DONE, INV>(g, x, tw, [&](int idx, cx<T> v) { fin(y, idx, v); });
+    g.sync();
+    return y;
+  } else {
+    stockham_pass<T, LOGN, LGR, DONE, INV>(g, x, tw, [&](int idx, cx<T> v) { y[fpad(idx)] = v; });
+    g.sync();
+    return fft_ct_passes<T, LOGN, P + 1, INV>(g, y, x, tw, fin);
+  }
+}
+
+// FFT of 2^LOGN points held in `a` at padded positions fpad(i) (`b` is scratch of the same
+// size).  The final pass hands every output to fin(y, index, value), where y is the buffer
+// that pass does not read and `index` the unpadded output index; returns y.  All group
+// threads call.
+template <class T, int LOGN, bool INV, class FinalStore>
+RK_DEV cx<T>* fft_ct(const Group& g, cx<T>* a, cx<T>* b, const cx<T>* tw, FinalStore fin) {
+  return fft_ct_passes<T, LOGN, 0, INV>(g, a, b, tw, fin);
+}
+
+template <class T>
+struct StoreY {
+  RK_DEV void operator()(cx<T>* y, int idx, cx<T> v) const { y[fpad(idx)] = v; }
+};
+
+}  // namespace rk

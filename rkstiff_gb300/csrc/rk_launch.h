@@ -11,8 +11,23 @@ namespace rk {
 void set_error(const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 
-#define RK_DECLARE_METHOD(NAME)                                                      \
-  int launch_evolve_##NAME(const rk_batch& b, cudaStream_t s);                       \
+// One launch of the evolve kernel over `count` items of `order`, all of grid size n
+// (n = 0: mixed sizes up to b.n_max, runtime-size kernel).
+struct ClassLaunch {
+  const int32_t* order;
+  int64_t count;
+  int32_t n;       // class grid size, 0 for mixed
+  int32_t* queue;  // work counter (zeroed by the launcher)
+  int threads;     // threads per instance (> 0)
+  int place;       // RK_PLACE_GLOBAL / SMEM_STATE / SMEM_ALL (resolved, not AUTO)
+};
+
+// Shared-memory bytes a class launch needs, or 0 when the placement does not fit.
+size_t class_smem_bytes(const rk_batch& b, int n, int place);
+
+#define RK_DECLARE_METHOD(NAME)                                                                   \
+  int launch_evolve_##NAME(const rk_batch& b, const ClassLaunch& c, cudaStream_t s);              \
+  size_t smem_bytes_##NAME(const rk_batch& b, int n, int place);                                  \
   int launch_coeffs_##NAME(int precision, int coef_complex, int64_t m, const double* lin, double h, \
                            const rk_etd_config& etd, void* out, cudaStream_t s);
 
@@ -23,5 +38,9 @@ RK_DECLARE_METHOD(IF45DP)
 RK_DECLARE_METHOD(ETD4)
 RK_DECLARE_METHOD(ETD5)
 RK_DECLARE_METHOD(IF4)
+
+// compile-time-size ETD35 kernels for real operators (rk_m_etd35_ct.cu); returns
+// RK_E_UNSUPPORTED when no specialisation exists for (precision, n)
+int launch_evolve_etd35_ct(const rk_batch& b, const ClassLaunch& c, cudaStream_t s);
 
 }  // namespace rk

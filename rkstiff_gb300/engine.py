@@ -142,8 +142,15 @@ class DiagEnsemble:
             self.kx_dev = None
         self.n_dev = torch.from_numpy(self.ns).to(dev)
         self.off_dev = torch.from_numpy(self.mode_off).to(dev)
+        # largest grids first; instances of equal n form one class (one kernel each)
         order = np.argsort(-self.ns, kind="stable").astype(np.int32)
         self.order_dev = torch.from_numpy(order).to(dev)
+        sorted_n = self.ns[order]
+        bounds = [0] + [i for i in range(1, n_inst) if sorted_n[i] != sorted_n[i - 1]] + [n_inst]
+        self.class_n = np.ascontiguousarray([int(sorted_n[b]) for b in bounds[:-1]], dtype=np.int32)
+        self.class_start = np.ascontiguousarray(bounds, dtype=np.int64)
+        self.class_threads = None  # per-class threads (np.int32) or None: library default
+        self.class_place = None    # per-class placement (np.int32) or None: library default
         sizes = [int(self.lib.rk_slab_bytes(self.method, self.prec, self.coef_complex, int(m))) for m in ms]
         offs = np.zeros(n_inst, dtype=np.int64)
         acc = 0
@@ -154,7 +161,7 @@ class DiagEnsemble:
         self.slab = torch.empty(max(acc, 256), dtype=torch.uint8, device=dev)
         self.slab_off_dev = torch.from_numpy(offs).to(dev)
         self.state_dev = torch.zeros(n_inst * nat.STATE_DTYPE.itemsize, dtype=torch.uint8, device=dev)
-        self.queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.queue = torch.zeros(max(1, len(self.class_n)), dtype=torch.int32, device=dev)
         self.tw = twiddles(dev, self.prec)
         self.cdtype = complex_dtype(self.prec)
         self.set_config(config, etd_config)
@@ -245,6 +252,12 @@ class DiagEnsemble:
         b.threads = self.threads
         b.ctl = self.ctl
         b.etd = self.etd
+        b.n_classes = len(self.class_n)
+        b.placement = nat.RK_PLACE_AUTO
+        b.class_n = self.class_n.ctypes.data
+        b.class_start = self.class_start.ctypes.data
+        b.class_threads = self.class_threads.ctypes.data if self.class_threads is not None else None
+        b.class_place = self.class_place.ctypes.data if self.class_place is not None else None
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
             if self.record_events:

@@ -52,6 +52,14 @@ class Ensemble:
                                    precision=precision, config=config, etd_config=etd_config, device=device,
                                    threads=threads)
         self.state = None
+        self._lin_ops = list(lin_ops)
+        self._kxs = kxs
+
+    def autotune(self, u0s: Sequence, span: float, **kw) -> dict:
+        """Pick threads and scratch placement per grid-size class by timing candidates on
+        a sample of each class over ``span`` of simulated time (see rkstiff_gb300.autotune)."""
+        from . import autotune
+        return autotune.tune(self.engine, u0s, self._lin_ops, self._kxs, span, **kw)
 
     @property
     def n_inst(self) -> int:
