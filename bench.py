@@ -326,9 +326,9 @@ def gpu_arm(args, rank, world, cpu_line):
             "l2_flush": "not needed: per-step working set (%d MB scratch + states) exceeds the 126 MB L2"
                         % (eng.slab_bytes // (1 << 20)),
             "instance_status": counts,
-            "launch_shapes": {str(n): "%d threads, %s" % (v["threads"], {-1: "auto", 0: "global", 1: "smem-state",
-                                                                          2: "smem-all"}[v["place"]])
-                              for n, v in tuned.items()},
+            "launch_shapes": {str(n): "%d groups x %d threads per block, %s scratch" % (
+                v["groups"], v["threads"], {0: "global", 1: "smem-state", 2: "smem-all"}[v["place"]])
+                for n, v in tuned.items()},
         },
         "roofline": {
             "bound": "fp32",

@@ -130,7 +130,7 @@ typedef struct rk_batch {
   double* snap_t;          /* [device] snap_cap times per instance                     */
   int64_t max_steps;       /* accepted steps per instance per launch (safety bound)    */
   int32_t run_mode;        /* RK_RUN_EVOLVE / RK_RUN_STEP                              */
-  int32_t threads;         /* threads per instance group, a multiple of 32 <= 256 (0: auto) */
+  int32_t threads;         /* threads per instance group: 32, 64, 128 or 256 (0: auto)  */
   rk_controller ctl;
   rk_etd_config etd;
   /* Optional split of `order` into classes of equal grid size, each launched as its own
@@ -143,6 +143,7 @@ typedef struct rk_batch {
   const int64_t* class_start;   /* [host] n_classes+1 offsets into `order`                */
   const int32_t* class_threads; /* [host] threads per instance per class (NULL: auto)     */
   const int32_t* class_place;   /* [host] placement per class (NULL: `placement`)         */
+  const int32_t* class_groups;  /* [host] instance groups per block per class (NULL: auto) */
 } rk_batch;
 
 /* where an instance's scratch arrays live during a launch */

@@ -54,6 +54,7 @@ class RkBatch(ctypes.Structure):
         ("n_classes", ctypes.c_int32), ("placement", ctypes.c_int32),
         ("class_n", ctypes.c_void_p), ("class_start", ctypes.c_void_p),
         ("class_threads", ctypes.c_void_p), ("class_place", ctypes.c_void_p),
+        ("class_groups", ctypes.c_void_p),
     ]
 
 

@@ -20,10 +20,11 @@ import torch
 from . import _native as nat
 from .engine import DiagEnsemble
 
-THREADS = (64, 128, 256)
+# (threads per instance group, groups per block)
+SHAPES = ((32, 4), (32, 8), (64, 2), (64, 4), (128, 1), (128, 2), (256, 1))
 PLACES = (nat.RK_PLACE_SMEM_ALL, nat.RK_PLACE_SMEM_STATE, nat.RK_PLACE_GLOBAL)
 
-_CACHE: Dict[Tuple, Tuple[int, int]] = {}
+_CACHE: Dict[Tuple, Tuple[int, int, int]] = {}
 
 
 def _key(eng: DiagEnsemble, n: int) -> Tuple:
@@ -31,7 +32,7 @@ def _key(eng: DiagEnsemble, n: int) -> Tuple:
 
 
 def save(path: str) -> None:
-    data = [{"key": list(k), "threads": v[0], "place": v[1]} for k, v in _CACHE.items()]
+    data = [{"key": list(k), "threads": v[0], "place": v[1], "groups": v[2]} for k, v in _CACHE.items()]
     with open(path, "w") as f:
         json.dump(data, f, indent=1)
 
@@ -42,14 +43,15 @@ def load(path: str) -> int:
     with open(path) as f:
         data = json.load(f)
     for item in data:
-        _CACHE[tuple(item["key"])] = (int(item["threads"]), int(item["place"]))
+        _CACHE[tuple(item["key"])] = (int(item["threads"]), int(item["place"]), int(item.get("groups", 1)))
     return len(data)
 
 
 def _time_candidate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, threads: int, place: int,
-                    reps: int) -> Optional[float]:
+                    groups: int, reps: int) -> Optional[float]:
     sub.class_threads = np.full(len(sub.class_n), threads, dtype=np.int32)
     sub.class_place = np.full(len(sub.class_n), place, dtype=np.int32)
+    sub.class_groups = np.full(len(sub.class_n), groups, dtype=np.int32)
     u = torch.empty_like(u0)
     best = None
     for _ in range(reps + 1):
@@ -70,8 +72,9 @@ def _time_candidate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, 
 
 def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequence], span: float,
          h_init: Optional[float] = None, sample: Optional[int] = None, reps: int = 1,
-         threads: Sequence[int] = THREADS, places: Sequence[int] = PLACES, force: bool = False) -> Dict[int, dict]:
-    """Choose (threads, placement) per class of ``eng`` and install them on it.
+         shapes: Sequence[Tuple[int, int]] = SHAPES, places: Sequence[int] = PLACES,
+         force: bool = False) -> Dict[int, dict]:
+    """Choose (threads, groups per block, placement) per class of ``eng`` and install them.
 
     ``u0s``/``lin_ops``/``kxs`` are the ensemble's per-instance inputs (host arrays),
     ``span`` the simulated time each trial integrates.  Returns {n: {threads, place,
@@ -79,14 +82,15 @@ def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequ
     nsm = torch.cuda.get_device_properties(eng.device).multi_processor_count
     sample = sample or 4 * nsm
     h = h_init if h_init is not None else span / 100.0
-    chosen_t, chosen_p, report = [], [], {}
+    chosen_t, chosen_p, chosen_g, report = [], [], [], {}
     for n in eng.class_n:
         key = _key(eng, n)
         if key in _CACHE and not force:
-            t, p = _CACHE[key]
+            t, p, gr = _CACHE[key]
             chosen_t.append(t)
             chosen_p.append(p)
-            report[int(n)] = {"threads": t, "place": p, "cached": True}
+            chosen_g.append(gr)
+            report[int(n)] = {"threads": t, "place": p, "groups": gr, "cached": True}
             continue
         idx = [i for i in range(eng.n_inst) if eng.ns[i] == n][:sample]
         sub = DiagEnsemble(eng.method_name, [lin_ops[i] for i in idx], eng.nl_kind, eng.nl_coef,
@@ -96,18 +100,21 @@ def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequ
         sub.ctl, sub.etd = eng.ctl, eng.etd
         u0 = sub.pack_u([u0s[i] for i in idx])
         rates = {}
-        for t in threads:
+        for t, gr in shapes:
             for p in places:
-                r = _time_candidate(sub, u0, span, h, t, p, reps)
+                r = _time_candidate(sub, u0, span, h, t, p, gr, reps)
                 if r is not None:
-                    rates[(t, p)] = r
+                    rates[(t, gr, p)] = r
         if not rates:
             raise RuntimeError(f"no launch shape fits grid size {n}")
-        (t, p), _ = max(rates.items(), key=lambda kv: kv[1])
-        _CACHE[key] = (t, p)
+        (t, gr, p), _ = max(rates.items(), key=lambda kv: kv[1])
+        _CACHE[key] = (t, p, gr)
         chosen_t.append(t)
         chosen_p.append(p)
-        report[int(n)] = {"threads": t, "place": p, "rates": {f"{a}/{b}": v for (a, b), v in rates.items()}}
+        chosen_g.append(gr)
+        report[int(n)] = {"threads": t, "place": p, "groups": gr,
+                          "rates": {f"{a}x{c}/{b}": v for (a, c, b), v in rates.items()}}
     eng.class_threads = np.asarray(chosen_t, dtype=np.int32)
     eng.class_place = np.asarray(chosen_p, dtype=np.int32)
+    eng.class_groups = np.asarray(chosen_g, dtype=np.int32)
     return report

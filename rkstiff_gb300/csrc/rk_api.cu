@@ -117,8 +117,13 @@ static int auto_threads(int n) {
   return t;
 }
 
+// groups per block: a block of about 128 threads
+static int auto_groups(int threads) { return threads >= 128 ? 1 : 128 / threads; }
+
 static int launch_class(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
-  if (smem_bytes_method(b, c.n > 0 ? c.n : b.n_max, c.place) > max_smem_per_block()) {
+  const int nn = c.n > 0 ? c.n : b.n_max;
+  const size_t tw_bytes = (size_t)nn * (b.precision == RK_FP64 ? 16 : 8);  // compile-time kernels' table
+  if (smem_bytes_method(b, nn, c.place) * (size_t)c.groups + tw_bytes > max_smem_per_block()) {
     set_error("rk_evolve: placement " + std::to_string(c.place) + " needs more shared memory than a block has");
     return RK_E_SIZE;
   }
@@ -243,8 +248,8 @@ int rk_evolve(const rk_batch* b, void* stream) {
     set_error("rk_evolve: contour_points must be > 1");
     return RK_E_ARG;
   }
-  if (b->threads < 0 || b->threads % 32 || b->threads > 256) {
-    set_error("rk_evolve: threads must be 0 (auto) or a multiple of 32 <= 256");
+  if (b->threads != 0 && b->threads != 32 && b->threads != 64 && b->threads != 128 && b->threads != 256) {
+    set_error("rk_evolve: threads must be 0 (auto), 32, 64, 128 or 256");
     return RK_E_ARG;
   }
   if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_ALL) {
@@ -253,8 +258,9 @@ int rk_evolve(const rk_batch* b, void* stream) {
   }
   cudaStream_t s = (cudaStream_t)stream;
   if (b->n_classes <= 0) {
-    ClassLaunch c{b->order, b->n_inst, 0, b->queue, b->threads > 0 ? b->threads : auto_threads(nmax),
-                  b->placement == RK_PLACE_AUTO ? auto_place(*b, nmax) : b->placement};
+    const int thr = b->threads > 0 ? b->threads : auto_threads(nmax);
+    ClassLaunch c{b->order, b->n_inst, 0, b->queue, thr,
+                  b->placement == RK_PLACE_AUTO ? auto_place(*b, nmax) : b->placement, 1};
     return launch_class(*b, c, s);
   }
   if (!b->class_n || !b->class_start) {
@@ -274,8 +280,13 @@ int rk_evolve(const rk_batch* b, void* stream) {
       return RK_E_SIZE;
     }
     int thr = b->class_threads ? b->class_threads[c] : (b->threads > 0 ? b->threads : auto_threads(n));
-    if (thr <= 0 || thr % 32 || thr > 256) {
-      set_error("rk_evolve: class thread counts must be multiples of 32 <= 256");
+    if (thr != 32 && thr != 64 && thr != 128 && thr != 256) {
+      set_error("rk_evolve: class thread counts must be 32, 64, 128 or 256");
+      return RK_E_ARG;
+    }
+    int grp = b->class_groups ? b->class_groups[c] : auto_groups(thr);
+    if (grp < 1 || thr * grp > 256 || (thr > 32 && grp > 15)) {
+      set_error("rk_evolve: class groups must be >= 1 with threads * groups <= 256");
       return RK_E_ARG;
     }
     int pl = b->class_place ? b->class_place[c] : b->placement;
@@ -284,7 +295,7 @@ int rk_evolve(const rk_batch* b, void* stream) {
       set_error("rk_evolve: unknown class placement");
       return RK_E_ARG;
     }
-    if (cnt > 0) cls.push_back(ClassLaunch{b->order + b->class_start[c], cnt, n, b->queue + c, thr, pl});
+    if (cnt > 0) cls.push_back(ClassLaunch{b->order + b->class_start[c], cnt, n, b->queue + c, thr, pl, grp});
   }
   if (cls.size() == 1) return launch_class(*b, cls[0], s);
   int dev = 0;

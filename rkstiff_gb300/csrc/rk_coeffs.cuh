@@ -53,6 +53,11 @@ RK_DEV cx<double> contour_node(const EtdCfg& c, int j) {
   return cx<double>{c.R * co, c.R * s};
 }
 
+template <class S> RK_DEV S from_d(double v);
+template <> RK_DEV double from_d<double>(double v) { return v; }
+template <> RK_DEV cx<double> from_d<cx<double>>(double v) { return cx<double>{v, 0.0}; }
+RK_DEV cx<double> operator+(cx<double> a, double b) { return cx<double>{a.x + b, a.y}; }
+
 template <class S> RK_DEV S from_cx(cx<double> v);
 template <> RK_DEV double from_cx<double>(cx<double> v) { return v.x; }
 template <> RK_DEV cx<double> from_cx<cx<double>>(cx<double> v) { return v; }
@@ -269,6 +274,52 @@ RK_DEV void fast_real_psi(int method, double z, double h, double* E, double* P) 
   } else {
     psis(0.5 * z, E[1], 2.0 * rz, P + 0, false);
     psis(z, E[3], rz, P + 2, true);
+  }
+}
+
+// psi_1..3 of a small argument by their Taylor series, used for coefficients stored in
+// FP32 in place of the contour mean (both evaluate the same functions to FP64 accuracy).
+// With S_k(x) = sum_{j>=0} x^j/(j+k)!: psi_1 = S_1, psi_2 = 2 S_2, psi_3 = 6 S_3 and
+// S_1 = 1 + x S_2, S_2 = 1/2 + x S_3.  S_3 is summed by Horner's rule through j = 21,
+// below FP64 resolution for |x| <= 1 (ETDConfig caps modecutoff at 1).
+template <class S>
+RK_DEV void taylor_s123(S x, S& s1, S& s2, S& s3) {
+  // inverse factorials 1/k! for k = 3..24, from the recurrence (no table of constants)
+  double inv[22];
+  inv[0] = 1.0 / 6.0;
+#pragma unroll
+  for (int k = 1; k < 22; ++k) inv[k] = inv[k - 1] / (double)(k + 3);
+  S acc = from_d<S>(inv[21]);
+#pragma unroll
+  for (int k = 20; k >= 0; --k) acc = from_d<S>(inv[k]) + x * acc;
+  s3 = acc;
+  s2 = from_d<S>(0.5) + x * s3;
+  s1 = from_d<S>(1.0) + x * s2;
+}
+
+// Small-mode psi set (same slots as the direct evaluation) and the exponentials
+// E = {e^{z/4}, e^{z/2}, e^{3z/4}, e^z}.
+template <class S>
+RK_DEV void taylor_psi(int method, S z, double h, S* E, S* P) {
+  E[0] = sexp(rdiv(z, 4.0));
+  E[1] = sexp(rdiv(z, 2.0));
+  E[2] = sexp(rdiv(3.0 * z, 4.0));
+  E[3] = sexp(z);
+  auto put = [&](S x, S* out, bool third) {
+    S s1, s2, s3;
+    taylor_s123(x, s1, s2, s3);
+    out[0] = h * s1;
+    out[1] = h * (2.0 * s2);
+    if (third) out[2] = h * (6.0 * s3);
+  };
+  if (method == RK_ETD35 || method == RK_ETD5) {
+    put(rdiv(z, 4.0), P + 0, false);
+    put(rdiv(z, 2.0), P + 2, false);
+    put(rdiv(3.0 * z, 4.0), P + 4, false);
+    put(z, P + 6, true);
+  } else {
+    put(rdiv(z, 2.0), P + 0, false);
+    put(z, P + 2, true);
   }
 }
 

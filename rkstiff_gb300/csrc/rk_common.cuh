@@ -71,15 +71,99 @@ template <class T> RK_DEV cx<T> ld(const cx<T>* p, int64_t i) { return p[i]; }
 struct Group {
   int tid;    // rank inside the group
   int nthr;   // threads in the group
-  int bar;    // hardware barrier id
+  int bar;    // 0: the whole block (__syncthreads); > 0: named barrier; < 0: one warp
   RK_DEV void sync() const {
     if (bar == 0) {
       __syncthreads();
+    } else if (bar < 0) {
+      __syncwarp();
     } else {
       asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthr) : "memory");
     }
   }
 };
+
+// ---------------------------------------------------------------------------------
+// double-float sums: (hi, lo) FP32 pairs with error-free addition (Knuth's TwoSum), a
+// 48-bit-significand accumulator that needs no FP64 instruction.
+// ---------------------------------------------------------------------------------
+struct df {
+  float hi, lo;
+};
+RK_DEV df df_add(df a, df b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);
+  const float lo = err + a.lo + b.lo;
+  const float hi = s + lo;
+  return df{hi, lo - (hi - s)};
+}
+RK_DEV df df_add(df a, float b) { return df_add(a, df{b, 0.f}); }
+RK_DEV df warp_sum_df(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    df w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  return v;
+}
+RK_DEV float warp_max_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// group-wide double-float sums of two values (FP32 instructions only); the results are
+// returned as FP64 (hi + lo)
+RK_DEV void group_sum2_df(const Group& g, double* red, df a, df b, double& sa, double& sb) {
+  a = warp_sum_df(a);
+  b = warp_sum_df(b);
+  const int nw = g.nthr >> 5;
+  if (nw == 1) {
+    sa = (double)a.hi + (double)a.lo;
+    sb = (double)b.hi + (double)b.lo;
+    return;
+  }
+  float* rf = reinterpret_cast<float*>(red);
+  const int w = g.tid >> 5;
+  g.sync();
+  if ((g.tid & 31) == 0) {
+    rf[4 * w] = a.hi;
+    rf[4 * w + 1] = a.lo;
+    rf[4 * w + 2] = b.hi;
+    rf[4 * w + 3] = b.lo;
+  }
+  g.sync();
+  df ta{0.f, 0.f}, tb{0.f, 0.f};
+  for (int i = 0; i < nw; ++i) {
+    ta = df_add(ta, df{rf[4 * i], rf[4 * i + 1]});
+    tb = df_add(tb, df{rf[4 * i + 2], rf[4 * i + 3]});
+  }
+  sa = (double)ta.hi + (double)ta.lo;
+  sb = (double)tb.hi + (double)tb.lo;
+}
+
+// group-wide max of a non-negative FP32 value; NaN anywhere gives NaN
+RK_DEV float group_max_nan_f(const Group& g, double* red, float v, bool nan) {
+  v = warp_max_f(nan ? 0.f : v);
+  const unsigned anynan = __ballot_sync(0xffffffffu, nan);
+  const int nw = g.nthr >> 5;
+  if (nw == 1) return anynan ? __int_as_float(0x7fc00000) : v;
+  float* rf = reinterpret_cast<float*>(red);
+  const int w = g.tid >> 5;
+  g.sync();
+  if ((g.tid & 31) == 0) {
+    rf[2 * w] = v;
+    rf[2 * w + 1] = anynan ? 1.f : 0.f;
+  }
+  g.sync();
+  float m = 0.f, f = 0.f;
+  for (int i = 0; i < nw; ++i) {
+    m = fmaxf(m, rf[2 * i]);
+    f = fmaxf(f, rf[2 * i + 1]);
+  }
+  return f > 0.f ? __int_as_float(0x7fc00000) : m;
+}
 
 // Reductions over a group through a small shared scratch (>= 32 doubles per group).
 RK_DEV double warp_sum(double v) {

@@ -65,7 +65,8 @@ struct Ctx {
   cx<T>* fa;
   cx<T>* fb;
   double* red;
-  const cx<T>* tw;
+  const cx<T>* tw;   // global table of RK_TW_N twiddles
+  const cx<T>* tws;  // compile-time path: shared-memory table of 2^LOGN twiddles
   RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
 };
 
@@ -84,27 +85,42 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     const int n = LOGN > 0 ? (1 << LOGN) : x.n, M = n >> 1;
     const T inv_n = T(1) / T(n);
     cx<T>* Z = x.fa;
-    for (int j = g.tid; j <= M; j += g.nthr) {
-      cx<T> k = kf(j);
-      cx<T> A = k * inv_n;
-      cx<T> B = mul_i(k) * (T(x.kx[j]) * inv_n);
-      if (j == 0 || j == M) {
-        A.y = T(0);
-        B.y = T(0);
+    // the stage values of PK modes are formed (all their loads issued) before any store
+    constexpr int PK = 4;
+    for (int j0 = g.tid; j0 <= M; j0 += PK * g.nthr) {
+      cx<T> kv[PK];
+      T kxv[PK];
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * g.nthr;
+        const bool in = j <= M;
+        kv[q] = in ? kf(j) : cx<T>{T(0), T(0)};
+        kxv[q] = in ? T(x.kx[j]) : T(0);
       }
-      Z[P(j)] = cx<T>{A.x - B.y, A.y + B.x};
-      if (j > 0 && j < M) Z[P(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * g.nthr;
+        if (j > M) break;
+        cx<T> A = kv[q] * inv_n;
+        cx<T> B = mul_i(kv[q]) * (kxv[q] * inv_n);
+        if (j == 0 || j == M) {
+          A.y = T(0);
+          B.y = T(0);
+        }
+        Z[P(j)] = cx<T>{A.x - B.y, A.y + B.x};
+        if (j > 0 && j < M) Z[P(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
+      }
     }
     g.sync();
     cx<T>* F;
     if constexpr (LOGN > 0) {
       // last inverse pass writes the real product u*ux; the forward transform of
       // length n/2 reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
-      cx<T>* w = fft_ct<T, LOGN, true>(g, x.fa, x.fb, x.tw, [](cx<T>* y, int idx, cx<T> v) {
+      cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, x.fa, x.fb, x.tws, [](cx<T>* y, int idx, cx<T> v) {
         reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
       });
       cx<T>* other = (w == x.fa) ? x.fb : x.fa;
-      F = fft_ct<T, LOGN - 1, false>(g, w, other, x.tw, StoreY<T>());
+      F = fft_ct<T, LOGN - 1, false, LOGN>(g, w, other, x.tws, StoreY<T>());
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
@@ -116,31 +132,57 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
       g.sync();
       F = fft_group<T, false>(g, other, z, x.logn - 1, x.tw);
     }
-    // rfft of the real product from the length-n/2 transform (split formula)
-    const int tws = LOGN > 0 ? (RK_TW_N >> LOGN) : (RK_TW_N >> x.logn);
-    for (int k = g.tid; k <= M; k += g.nthr) {
-      cx<T> Fk = F[P(k == M ? 0 : k)];
-      cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
-      cx<T> Fe = (Fk + Fm) * T(0.5);
-      cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-      cx<T> W = Fe + x.tw[k * tws] * Fo;
-      out[k] = W * x.nl_c;
+    // rfft of the real product from the length-n/2 transform (split formula);
+    // exp(-2 pi i k/n) from the n-point shared table (compile-time path) or the global one
+    const cx<T>* twu = LOGN > 0 ? x.tws : x.tw;
+    const int tws = LOGN > 0 ? 1 : (RK_TW_N >> x.logn);
+    for (int k0 = g.tid; k0 <= M; k0 += PK * g.nthr) {
+      cx<T> W[PK];
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int k = k0 + q * g.nthr;
+        if (k > M) break;
+        cx<T> Fk = F[P(k == M ? 0 : k)];
+        cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
+        cx<T> Fe = (Fk + Fm) * T(0.5);
+        cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[k * tws]) * Fo;
+      }
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int k = k0 + q * g.nthr;
+        if (k > M) break;
+        out[k] = W[q] * x.nl_c;
+      }
     }
     g.sync();
   } else if (x.nl_kind == RK_NL_NLS) {
     // v = ifft(k); N = fft(i c |v|^2 v)
     const int n = LOGN > 0 ? (1 << LOGN) : x.n;
     const T inv_n = T(1) / T(n);
-    for (int j = g.tid; j < n; j += g.nthr) x.fa[P(j)] = kf(j) * inv_n;
+    constexpr int PK = 4;
+    for (int j0 = g.tid; j0 < n; j0 += PK * g.nthr) {
+      cx<T> kv[PK];
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * g.nthr;
+        kv[q] = j < n ? kf(j) : cx<T>{T(0), T(0)};
+      }
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * g.nthr;
+        if (j < n) x.fa[P(j)] = kv[q] * inv_n;
+      }
+    }
     g.sync();
     const T c = x.nl_c;
     if constexpr (LOGN > 0) {
-      cx<T>* w = fft_ct<T, LOGN, true>(g, x.fa, x.fb, x.tw, [c](cx<T>* y, int idx, cx<T> v) {
+      cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, x.fa, x.fb, x.tws, [c](cx<T>* y, int idx, cx<T> v) {
         T a2 = (v.x * v.x + v.y * v.y) * c;
         y[fpad(idx)] = cx<T>{-a2 * v.y, a2 * v.x};
       });
       cx<T>* other = (w == x.fa) ? x.fb : x.fa;
-      fft_ct<T, LOGN, false>(g, w, other, x.tw, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
+      fft_ct<T, LOGN, false, LOGN>(g, w, other, x.tws, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
@@ -194,12 +236,24 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
-  // pass 1: thread per mode, direct formula for |z| >= modecutoff
+  // pass 1: thread per mode, direct formula for |z| >= modecutoff; with FAST the small
+  // modes are evaluated here too, by the Taylor series of psi_k (see taylor_psi)
   for (int j = g.tid; j < m; j += g.nthr) {
     S z = load_z<S>(lin, j, h);
-    if (sabs(z) < ec.cutoff) continue;
+    const bool small = sabs(z) < ec.cutoff;
+    if (small && !FAST) continue;
     S P[NP];
     S o[NC];
+    if constexpr (FAST) {
+      if (small) {
+        S E[4];
+        taylor_psi<S>(METHOD, z, h, E, P);
+        etd_from_psi_e<S>(METHOD, E, P, o);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+        continue;
+      }
+    }
     if constexpr (FAST && sizeof(S) == sizeof(double)) {
       double E[4];
       fast_real_psi(METHOD, sre(z), h, E, reinterpret_cast<double*>(P));
@@ -216,6 +270,10 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     }
 #pragma unroll
     for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+  }
+  if constexpr (FAST) {
+    g.sync();
+    return;
   }
   // pass 2: warp per small mode, lanes over the contour nodes (rkstiff/etd35.py:257-288)
   const int lane = g.tid & 31, warp = g.tid >> 5, nwarp = g.nthr >> 5;
@@ -283,14 +341,25 @@ RK_DEV double write_unew(const Ctx<T, CT, LOGN>& x, KF kf) {
     return group_max_nan(x.g, x.red, nan ? nan_d() : mx);
   } else {
     float mx = 0.f;
-    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
-      cx<T> v = kf(j);
-      x.unew[j] = v;
-      float a2 = v.x * v.x + v.y * v.y;
-      if (a2 != a2) nan = true;
-      else mx = fmaxf(mx, a2);
+    constexpr int PK = 4;
+    for (int j0 = x.g.tid; j0 < x.m; j0 += PK * x.g.nthr) {
+      cx<T> v[PK];
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * x.g.nthr;
+        v[q] = j < x.m ? kf(j) : cx<T>{T(0), T(0)};
+      }
+#pragma unroll
+      for (int q = 0; q < PK; ++q) {
+        const int j = j0 + q * x.g.nthr;
+        if (j >= x.m) break;
+        x.unew[j] = v[q];
+        float a2 = v[q].x * v[q].x + v[q].y * v[q].y;
+        if (a2 != a2) nan = true;
+        else mx = fmaxf(mx, a2);
+      }
     }
-    return group_max_nan(x.g, x.red, nan ? nan_d() : (double)mx);
+    return (double)group_max_nan_f(x.g, x.red, mx, nan);
   }
 }
 
@@ -312,20 +381,24 @@ RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const 
       }
     }
   } else {
-    // maxu holds max |unew|^2 here; NaN keeps every comparison false, as in the reference
+    // maxu holds max |unew|^2 here; NaN keeps every comparison false, as in the reference.
+    // The sums are carried in double-float (FP32 pairs with error-free addition, a
+    // 48-bit significand) and formed as FP64 once per group.
     const float thr = (float)(ctl.adapt_cutoff * ctl.adapt_cutoff * maxu);
+    df au{0.f, 0.f}, ae{0.f, 0.f};
     for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
       cx<T> v = x.unew[j];
       float a2 = v.x * v.x + v.y * v.y;
       if (a2 > thr) {
-        su += (double)a2;
+        au = df_add(au, a2);
         cx<T> e = ef(j);
-        se += (double)(e.x * e.x + e.y * e.y);
+        ae = df_add(ae, e.x * e.x + e.y * e.y);
       }
     }
+    group_sum2_df(x.g, x.red, au, ae, su, se);
   }
-  group_sum2(x.g, x.red, su, se);
   if constexpr (sizeof(T) == sizeof(double)) {
+    group_sum2(x.g, x.red, su, se);
     double tol = ctl.epsilon * sqrt(su);
     return ctl.safety_f * pow(tol / sqrt(se), 1.0 / q);
   } else {
@@ -525,7 +598,7 @@ enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
-                         unsigned char* sm_slab) {
+                         unsigned char* sm_slab, const cx<T>* tws) {
   using Tr = Traits<METHOD>;
   Ctx<T, CT, LOGN> x;
   x.g = g;
@@ -549,6 +622,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.fb = fb;
   x.red = red;
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
+  x.tws = tws;
   const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
   const rk_controller ctl = b.ctl;
 
@@ -670,18 +744,33 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   g.sync();
 }
 
-// Shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction scratch,
-// the work-item slot, then (PLACE > 0) the instance arrays for mp_s modes.
+// A block holds blockDim.x / gthreads independent groups; each group owns one slice of
+// shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction
+// scratch, the work-item slot, then (PLACE > 0) the instance arrays (group_smem bytes in
+// all).  Compile-time-size kernels put a block-wide table of the 2^LOGN twiddles after the
+// group slices.  A one-warp group synchronises with __syncwarp, a multi-warp group with a
+// named barrier (one per group), a block-wide group with __syncthreads.
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const int32_t* __restrict__ order,
-                                                        int64_t count, int32_t* queue, int nfft) {
+                                                        int64_t count, int32_t* queue, int nfft, int gthreads,
+                                                        int group_smem) {
   extern __shared__ __align__(16) unsigned char smem[];
-  cx<T>* fa = reinterpret_cast<cx<T>*>(smem);
+  const int ngroups = blockDim.x / gthreads;
+  const int gi = threadIdx.x / gthreads;
+  cx<T>* tws = nullptr;
+  if constexpr (LOGN > 0) {
+    tws = reinterpret_cast<cx<T>*>(smem + (size_t)ngroups * group_smem);
+    const cx<T>* tw = reinterpret_cast<const cx<T>*>(b.twiddle);
+    for (int j = threadIdx.x; j < (1 << LOGN); j += blockDim.x) tws[j] = tw[j * (RK_TW_N >> LOGN)];
+    __syncthreads();
+  }
+  unsigned char* base = smem + (size_t)gi * group_smem;
+  cx<T>* fa = reinterpret_cast<cx<T>*>(base);
   cx<T>* fb = fa + fpad_size(nfft);
   double* red = reinterpret_cast<double*>(fb + fpad_size(nfft));
   int* item_s = reinterpret_cast<int*>(red + 64);
   unsigned char* sm_slab = reinterpret_cast<unsigned char*>(red + 66);
-  Group g{(int)threadIdx.x, (int)blockDim.x, 0};
+  const Group g{(int)(threadIdx.x % gthreads), gthreads, gthreads == 32 ? -1 : (ngroups == 1 ? 0 : 1 + gi)};
   for (;;) {
     if (g.tid == 0) *item_s = atomicAdd(queue, 1);
     g.sync();
@@ -689,7 +778,7 @@ __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const 
     g.sync();
     if (item >= count) break;
     const int inst = order ? order[item] : item;
-    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab);
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws);
   }
 }
 

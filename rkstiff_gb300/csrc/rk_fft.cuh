@@ -212,10 +212,10 @@ struct PassRadix {
 
 // One Stockham pass of radix R = 2^LGR at sub-length Ls = 2^LGLS over N = 2^LOGN points.
 // `post(idx, value)` receives the output (final pass) -- by default a store to y.
-template <class T, int LOGN, int LGR, int LGLS, bool INV, class Store>
+template <class T, int LOGN, int LGR, int LGLS, bool INV, int TWLOG, class Store>
 RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ tw, Store store) {
   constexpr int N = 1 << LOGN, R = 1 << LGR, Ls = 1 << LGLS, NB = N / R;
-  constexpr int TWS = RK_TW_N >> (LGLS + LGR);  // table stride of W_{R Ls}
+  constexpr int TWS = (1 << TWLOG) >> (LGLS + LGR);  // table stride of W_{R Ls}
   for (int i = g.tid; i < NB; i += g.nthr) {
     const int k = i & (Ls - 1);
     cx<T> v[R];
@@ -232,29 +232,30 @@ RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<
   }
 }
 
-template <class T, int LOGN, int P, bool INV, class FinalStore>
+template <class T, int LOGN, int P, bool INV, int TWLOG, class FinalStore>
 RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw, FinalStore fin) {
   constexpr int LGR = PassRadix<LOGN, P>::used();
   constexpr int DONE = PassRadix<LOGN, P>::bits_before();
   if constexpr (DONE + LGR == LOGN) {
     // final pass: outputs go to fin(y, index, value); y is the buffer not being read
-    stockham_pass<T, LOGN, LGR, DONE, INV>(g, x, tw, [&](int idx, cx<T> v) { fin(y, idx, v); });
+    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, cx<T> v) { fin(y, idx, v); });
     g.sync();
     return y;
   } else {
-    stockham_pass<T, LOGN, LGR, DONE, INV>(g, x, tw, [&](int idx, cx<T> v) { y[fpad(idx)] = v; });
+    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, cx<T> v) { y[fpad(idx)] = v; });
     g.sync();
-    return fft_ct_passes<T, LOGN, P + 1, INV>(g, y, x, tw, fin);
+    return fft_ct_passes<T, LOGN, P + 1, INV, TWLOG>(g, y, x, tw, fin);
   }
 }
 
 // FFT of 2^LOGN points held in `a` at padded positions fpad(i) (`b` is scratch of the same
-// size).  The final pass hands every output to fin(y, index, value), where y is the buffer
-// that pass does not read and `index` the unpadded output index; returns y.  All group
-// threads call.
-template <class T, int LOGN, bool INV, class FinalStore>
+// size), with `tw` a table of the 2^TWLOG twiddles exp(-2 pi i k/2^TWLOG), TWLOG >= LOGN.
+// The final pass hands every output to fin(y, index, value), where y is the buffer that
+// pass does not read and `index` the unpadded output index; returns y.  All group threads
+// call.
+template <class T, int LOGN, bool INV, int TWLOG, class FinalStore>
 RK_DEV cx<T>* fft_ct(const Group& g, cx<T>* a, cx<T>* b, const cx<T>* tw, FinalStore fin) {
-  return fft_ct_passes<T, LOGN, 0, INV>(g, a, b, tw, fin);
+  return fft_ct_passes<T, LOGN, 0, INV, TWLOG>(g, a, b, tw, fin);
 }
 
 template <class T>

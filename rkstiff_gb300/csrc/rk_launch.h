@@ -18,8 +18,9 @@ struct ClassLaunch {
   int64_t count;
   int32_t n;       // class grid size, 0 for mixed
   int32_t* queue;  // work counter (zeroed by the launcher)
-  int threads;     // threads per instance (> 0)
+  int threads;     // threads per instance group (32, 64, 128 or 256)
   int place;       // RK_PLACE_GLOBAL / SMEM_STATE / SMEM_ALL (resolved, not AUTO)
+  int groups;      // instance groups per block (threads * groups <= 256)
 };
 
 // Shared-memory bytes a class launch needs, or 0 when the placement does not fit.

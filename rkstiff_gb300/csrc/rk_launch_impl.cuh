@@ -11,7 +11,9 @@ template <class T, class CT, class S, int M, int LOGN, int PLACE>
 static int launch_evolve_v(const rk_batch& b, const ClassLaunch& c, cudaStream_t st) {
   const int nfft = c.n > 0 ? c.n : b.n_max;
   const int64_t m = (b.nl_kind == RK_NL_UUX) ? nfft / 2 + 1 : nfft;
-  const size_t sm = evolve_smem<T>(nfft) + smem_slab_bytes<T, CT, M>(PLACE, m);
+  const size_t group_smem = (evolve_smem<T>(nfft) + smem_slab_bytes<T, CT, M>(PLACE, m) + 15) & ~size_t(15);
+  const size_t sm = group_smem * (size_t)c.groups + (LOGN > 0 ? (sizeof(cx<T>) << LOGN) : 0);
+  const int block = c.threads * c.groups;
   auto kern = evolve_kernel<T, CT, S, M, LOGN, PLACE>;
   if (int e = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
                          "cudaFuncSetAttribute(evolve smem)"))
@@ -19,17 +21,19 @@ static int launch_evolve_v(const rk_batch& b, const ClassLaunch& c, cudaStream_t
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (int e = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c.threads, sm), "occupancy"))
+  if (int e = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, sm), "occupancy"))
     return e;
   if (occ < 1) {
     set_error("evolve kernel does not fit on an SM (shared memory " + std::to_string(sm) + " bytes, " +
-              std::to_string(c.threads) + " threads)");
+              std::to_string(block) + " threads)");
     return RK_E_SIZE;
   }
+  // enough groups to cover the class, at most a full residency of the device
+  long need = (long)((c.count + c.groups - 1) / c.groups);
   long grid = (long)nsm * occ;
-  if ((long)c.count < grid) grid = (long)c.count;
+  if (need < grid) grid = need;
   if (int e = cuda_check(cudaMemsetAsync(c.queue, 0, sizeof(int32_t), st), "queue reset")) return e;
-  kern<<<(unsigned)grid, c.threads, sm, st>>>(b, c.order, c.count, c.queue, nfft);
+  kern<<<(unsigned)grid, block, sm, st>>>(b, c.order, c.count, c.queue, nfft, c.threads, (int)group_smem);
   return cuda_check(cudaGetLastError(), "evolve launch");
 }
 
@@ -44,20 +48,21 @@ static int launch_evolve_p(const rk_batch& b, const ClassLaunch& c, cudaStream_t
   return RK_E_ARG;
 }
 
+// shared memory of one instance group (the block holds `groups` of them)
 template <class T, class CT>
 static size_t smem_bytes_t(const rk_batch& b, int M, int n, int place) {
   const int64_t m = (b.nl_kind == RK_NL_UUX) ? n / 2 + 1 : n;
   size_t sm = evolve_smem<T>(n);
   switch (M) {
-    case RK_ETD35: return sm + smem_slab_bytes<T, CT, RK_ETD35>(place, m);
-    case RK_ETD5: return sm + smem_slab_bytes<T, CT, RK_ETD5>(place, m);
-    case RK_ETD34: return sm + smem_slab_bytes<T, CT, RK_ETD34>(place, m);
-    case RK_ETD4: return sm + smem_slab_bytes<T, CT, RK_ETD4>(place, m);
-    case RK_IF34: return sm + smem_slab_bytes<T, CT, RK_IF34>(place, m);
-    case RK_IF4: return sm + smem_slab_bytes<T, CT, RK_IF4>(place, m);
-    case RK_IF45DP: return sm + smem_slab_bytes<T, CT, RK_IF45DP>(place, m);
+    case RK_ETD35: sm += smem_slab_bytes<T, CT, RK_ETD35>(place, m); break;
+    case RK_ETD5: sm += smem_slab_bytes<T, CT, RK_ETD5>(place, m); break;
+    case RK_ETD34: sm += smem_slab_bytes<T, CT, RK_ETD34>(place, m); break;
+    case RK_ETD4: sm += smem_slab_bytes<T, CT, RK_ETD4>(place, m); break;
+    case RK_IF34: sm += smem_slab_bytes<T, CT, RK_IF34>(place, m); break;
+    case RK_IF4: sm += smem_slab_bytes<T, CT, RK_IF4>(place, m); break;
+    case RK_IF45DP: sm += smem_slab_bytes<T, CT, RK_IF45DP>(place, m); break;
   }
-  return 0;
+  return (sm + 15) & ~size_t(15);
 }
 
 template <int M>

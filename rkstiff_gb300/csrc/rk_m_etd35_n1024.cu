@@ -7,10 +7,11 @@ namespace rk {
 template <class T>
 static int ct_1024(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
   switch (c.place) {
+    case RK_PLACE_GLOBAL: return launch_evolve_v<T, T, double, RK_ETD35, 10, PL_GLOBAL>(b, c, s);
     case RK_PLACE_SMEM_STATE: return launch_evolve_v<T, T, double, RK_ETD35, 10, PL_SMEM_STATE>(b, c, s);
     case RK_PLACE_SMEM_ALL: return launch_evolve_v<T, T, double, RK_ETD35, 10, PL_SMEM_ALL>(b, c, s);
   }
-  return RK_E_UNSUPPORTED;  // global placement: the runtime-size kernel serves it
+  return RK_E_UNSUPPORTED;
 }
 
 int launch_evolve_etd35_n1024(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {

@@ -151,6 +151,7 @@ class DiagEnsemble:
         self.class_start = np.ascontiguousarray(bounds, dtype=np.int64)
         self.class_threads = None  # per-class threads (np.int32) or None: library default
         self.class_place = None    # per-class placement (np.int32) or None: library default
+        self.class_groups = None   # per-class instance groups per block (np.int32) or None
         sizes = [int(self.lib.rk_slab_bytes(self.method, self.prec, self.coef_complex, int(m))) for m in ms]
         offs = np.zeros(n_inst, dtype=np.int64)
         acc = 0
@@ -258,6 +259,7 @@ class DiagEnsemble:
         b.class_start = self.class_start.ctypes.data
         b.class_threads = self.class_threads.ctypes.data if self.class_threads is not None else None
         b.class_place = self.class_place.ctypes.data if self.class_place is not None else None
+        b.class_groups = self.class_groups.ctypes.data if self.class_groups is not None else None
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
             if self.record_events:

@@ -106,3 +106,4 @@ def test_ensemble_placements_agree():
         assert rel(run(thr, place), a) < 1e-5, (thr, place)
     eng.class_threads = None
     eng.class_place = None
+    eng.class_groups = None
