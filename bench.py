@@ -235,7 +235,13 @@ def gpu_arm(args, rank, world, cpu_line):
     ens = Ensemble("ETD35", lins, nls, config=SolverConfig(epsilon=WORKLOAD["epsilon"]), precision="fp32",
                    device=dev)
     eng = ens.engine
-    tuned = ens.autotune(u0s, span=2.0)
+    from rkstiff_gb300 import autotune as _at
+    if args.tune_cache and _at.load(args.tune_cache):
+        tuned = ens.autotune(u0s, span=10.0)  # served from the loaded cache
+    else:
+        tuned = ens.autotune(u0s, span=10.0)
+        if args.tune_cache:
+            _at.save(args.tune_cache)
     u0_dev = ens.pack(u0s)
     u = torch.empty_like(u0_dev)
     tf = WORKLOAD["tf"]
@@ -419,6 +425,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tune-cache", default="", help="JSON file of tuned launch shapes to load, or to write")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", 1))
     rank = int(os.environ.get("RANK", 0))

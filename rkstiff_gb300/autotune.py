@@ -1,9 +1,11 @@
 """Autotuner for the launch shape of each grid-size class of an ensemble.
 
-For every class (instances sharing one grid size, launched as one kernel) it times the
-candidate thread counts and scratch placements on a sample of that class's own instances
-over a short span of simulated time, and keeps the fastest.  Results are cached per
-(device, method, precision, operator kind, nonlinearity, n) for the process, and can be
+Each class (instances sharing one grid size) runs as its own kernel, concurrently with the
+other classes.  The tuner sweeps the classes in turn: for one class it times every
+candidate (threads per instance group, groups per block, scratch placement) while the
+other classes keep their current shapes, running a subsample of the whole ensemble over a
+short span of simulated time, and keeps the fastest.  Results are cached per (device,
+method, precision, operator kind, nonlinearity, grid-size mix) for the process and can be
 saved to / loaded from a JSON file.
 """
 
@@ -24,15 +26,16 @@ from .engine import DiagEnsemble
 SHAPES = ((32, 4), (32, 8), (64, 2), (64, 4), (128, 1), (128, 2), (256, 1))
 PLACES = (nat.RK_PLACE_SMEM_ALL, nat.RK_PLACE_SMEM_STATE, nat.RK_PLACE_GLOBAL)
 
-_CACHE: Dict[Tuple, Tuple[int, int, int]] = {}
+_CACHE: Dict[Tuple, Tuple[Tuple[int, int, int], ...]] = {}
 
 
-def _key(eng: DiagEnsemble, n: int) -> Tuple:
-    return (torch.cuda.get_device_name(eng.device), eng.method_name, eng.prec, eng.coef_complex, eng.nl_kind, int(n))
+def _key(eng: DiagEnsemble) -> Tuple:
+    return (torch.cuda.get_device_name(eng.device), eng.method_name, eng.prec, eng.coef_complex, eng.nl_kind,
+            tuple(int(n) for n in eng.class_n))
 
 
 def save(path: str) -> None:
-    data = [{"key": list(k), "threads": v[0], "place": v[1], "groups": v[2]} for k, v in _CACHE.items()]
+    data = [{"key": list(k), "shapes": [list(v) for v in vals]} for k, vals in _CACHE.items()]
     with open(path, "w") as f:
         json.dump(data, f, indent=1)
 
@@ -43,15 +46,18 @@ def load(path: str) -> int:
     with open(path) as f:
         data = json.load(f)
     for item in data:
-        _CACHE[tuple(item["key"])] = (int(item["threads"]), int(item["place"]), int(item.get("groups", 1)))
+        key = tuple(tuple(x) if isinstance(x, list) else x for x in item["key"])
+        _CACHE[key] = tuple(tuple(v) for v in item["shapes"])
     return len(data)
 
 
-def _time_candidate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, threads: int, place: int,
-                    groups: int, reps: int) -> Optional[float]:
-    sub.class_threads = np.full(len(sub.class_n), threads, dtype=np.int32)
-    sub.class_place = np.full(len(sub.class_n), place, dtype=np.int32)
-    sub.class_groups = np.full(len(sub.class_n), groups, dtype=np.int32)
+def _install(eng: DiagEnsemble, shapes) -> None:
+    eng.class_threads = np.asarray([s[0] for s in shapes], dtype=np.int32)
+    eng.class_groups = np.asarray([s[1] for s in shapes], dtype=np.int32)
+    eng.class_place = np.asarray([s[2] for s in shapes], dtype=np.int32)
+
+
+def _rate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, reps: int) -> Optional[float]:
     u = torch.empty_like(u0)
     best = None
     for _ in range(reps + 1):
@@ -61,60 +67,57 @@ def _time_candidate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, 
         try:
             st = sub.evolve(u, 0.0, span, h)
         except nat.NativeError:
-            return None  # the placement does not fit this size
+            return None  # a shape that does not fit this size
         torch.cuda.synchronize(sub.device)
-        dt = time.perf_counter() - t0
-        work = float(np.sum(sub.ms * st["steps"]))
-        rate = work / dt
+        rate = float(np.sum(sub.ms * st["steps"])) / (time.perf_counter() - t0)
         best = rate if best is None else max(best, rate)
     return best
 
 
 def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequence], span: float,
-         h_init: Optional[float] = None, sample: Optional[int] = None, reps: int = 1,
+         h_init: Optional[float] = None, per_class: Optional[int] = None, reps: int = 1,
          shapes: Sequence[Tuple[int, int]] = SHAPES, places: Sequence[int] = PLACES,
          force: bool = False) -> Dict[int, dict]:
     """Choose (threads, groups per block, placement) per class of ``eng`` and install them.
 
-    ``u0s``/``lin_ops``/``kxs`` are the ensemble's per-instance inputs (host arrays),
-    ``span`` the simulated time each trial integrates.  Returns {n: {threads, place,
-    rates}}."""
+    ``u0s``/``lin_ops``/``kxs`` are the ensemble's per-instance inputs (host arrays) and
+    ``span`` the simulated time of each trial.  Returns {n: {threads, groups, place, rates}}."""
+    key = _key(eng)
+    if key in _CACHE and not force:
+        chosen = list(_CACHE[key])
+        _install(eng, chosen)
+        return {int(n): {"threads": c[0], "groups": c[1], "place": c[2], "cached": True}
+                for n, c in zip(eng.class_n, chosen)}
     nsm = torch.cuda.get_device_properties(eng.device).multi_processor_count
-    sample = sample or 4 * nsm
-    h = h_init if h_init is not None else span / 100.0
-    chosen_t, chosen_p, chosen_g, report = [], [], [], {}
+    per_class = per_class or 2 * nsm
+    idx = []
     for n in eng.class_n:
-        key = _key(eng, n)
-        if key in _CACHE and not force:
-            t, p, gr = _CACHE[key]
-            chosen_t.append(t)
-            chosen_p.append(p)
-            chosen_g.append(gr)
-            report[int(n)] = {"threads": t, "place": p, "groups": gr, "cached": True}
-            continue
-        idx = [i for i in range(eng.n_inst) if eng.ns[i] == n][:sample]
-        sub = DiagEnsemble(eng.method_name, [lin_ops[i] for i in idx], eng.nl_kind, eng.nl_coef,
-                           None if kxs is None else [kxs[i] for i in idx], [int(n)] * len(idx),
-                           precision="fp64" if eng.prec == nat.RK_FP64 else "fp32", device=eng.device,
-                           complex_operator=bool(eng.coef_complex))
-        sub.ctl, sub.etd = eng.ctl, eng.etd
-        u0 = sub.pack_u([u0s[i] for i in idx])
+        idx += [i for i in range(eng.n_inst) if eng.ns[i] == n][:per_class]
+    sub = DiagEnsemble(eng.method_name, [lin_ops[i] for i in idx], eng.nl_kind, eng.nl_coef,
+                       None if kxs is None else [kxs[i] for i in idx], [int(eng.ns[i]) for i in idx],
+                       precision="fp64" if eng.prec == nat.RK_FP64 else "fp32", device=eng.device,
+                       complex_operator=bool(eng.coef_complex))
+    sub.ctl, sub.etd = eng.ctl, eng.etd
+    u0 = sub.pack_u([u0s[i] for i in idx])
+    h = h_init if h_init is not None else span / 100.0
+    assert list(sub.class_n) == list(eng.class_n)
+    chosen = [(128, 1, nat.RK_PLACE_GLOBAL)] * len(sub.class_n)
+    report = {}
+    for c, n in enumerate(sub.class_n):
         rates = {}
         for t, gr in shapes:
             for p in places:
-                r = _time_candidate(sub, u0, span, h, t, p, gr, reps)
+                trial = list(chosen)
+                trial[c] = (t, gr, p)
+                _install(sub, trial)
+                r = _rate(sub, u0, span, h, reps)
                 if r is not None:
                     rates[(t, gr, p)] = r
         if not rates:
             raise RuntimeError(f"no launch shape fits grid size {n}")
-        (t, gr, p), _ = max(rates.items(), key=lambda kv: kv[1])
-        _CACHE[key] = (t, p, gr)
-        chosen_t.append(t)
-        chosen_p.append(p)
-        chosen_g.append(gr)
-        report[int(n)] = {"threads": t, "place": p, "groups": gr,
-                          "rates": {f"{a}x{c}/{b}": v for (a, c, b), v in rates.items()}}
-    eng.class_threads = np.asarray(chosen_t, dtype=np.int32)
-    eng.class_place = np.asarray(chosen_p, dtype=np.int32)
-    eng.class_groups = np.asarray(chosen_g, dtype=np.int32)
+        chosen[c] = max(rates.items(), key=lambda kv: kv[1])[0]
+        report[int(n)] = {"threads": chosen[c][0], "groups": chosen[c][1], "place": chosen[c][2],
+                          "rates": {f"{a}x{b}/{p}": v for (a, b, p), v in rates.items()}}
+    _CACHE[key] = tuple(chosen)
+    _install(eng, chosen)
     return report

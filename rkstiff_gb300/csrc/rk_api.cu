@@ -100,12 +100,13 @@ static size_t max_smem_per_block() {
 // A single-step run keeps the coefficients in the global slab (they persist between
 // calls); an evolve may rebuild them in shared memory once per launch.
 static int auto_place(const rk_batch& b, int n) {
+  const size_t tw = (size_t)n * (b.precision == RK_FP64 ? 16 : 8);  // compile-time kernels' table
   const size_t lim1 = max_smem_per_block();
   const size_t lim2 = lim1 / 2 - 1024;
   const bool step = b.run_mode == RK_RUN_STEP;
   for (size_t lim : {lim2, lim1}) {
-    if (!step && smem_bytes_method(b, n, RK_PLACE_SMEM_ALL) <= lim) return RK_PLACE_SMEM_ALL;
-    if (smem_bytes_method(b, n, RK_PLACE_SMEM_STATE) <= lim) return RK_PLACE_SMEM_STATE;
+    if (!step && smem_bytes_method(b, n, RK_PLACE_SMEM_ALL) + tw <= lim) return RK_PLACE_SMEM_ALL;
+    if (smem_bytes_method(b, n, RK_PLACE_SMEM_STATE) + tw <= lim) return RK_PLACE_SMEM_STATE;
   }
   return RK_PLACE_GLOBAL;
 }

@@ -86,7 +86,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     const T inv_n = T(1) / T(n);
     cx<T>* Z = x.fa;
     // the stage values of PK modes are formed (all their loads issued) before any store
-    constexpr int PK = 4;
+    constexpr int PK = 1;
     for (int j0 = g.tid; j0 <= M; j0 += PK * g.nthr) {
       cx<T> kv[PK];
       T kxv[PK];
@@ -160,7 +160,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     // v = ifft(k); N = fft(i c |v|^2 v)
     const int n = LOGN > 0 ? (1 << LOGN) : x.n;
     const T inv_n = T(1) / T(n);
-    constexpr int PK = 4;
+    constexpr int PK = 1;
     for (int j0 = g.tid; j0 < n; j0 += PK * g.nthr) {
       cx<T> kv[PK];
 #pragma unroll
@@ -341,7 +341,7 @@ RK_DEV double write_unew(const Ctx<T, CT, LOGN>& x, KF kf) {
     return group_max_nan(x.g, x.red, nan ? nan_d() : mx);
   } else {
     float mx = 0.f;
-    constexpr int PK = 4;
+    constexpr int PK = 1;
     for (int j0 = x.g.tid; j0 < x.m; j0 += PK * x.g.nthr) {
       cx<T> v[PK];
 #pragma unroll
