@@ -46,10 +46,10 @@ METRIC = "mode-steps/s (KS uneven ensemble, ETD35 eps=1e-5, tf=100)"
 UNIT = "mode-steps/s"
 
 
-def make_instances(count: int, seed: int):
+def make_instances(count: int, seed: int, n_choices=None):
     """(n, L, u0_hat) per instance, seeded."""
     rng = np.random.default_rng(seed)
-    ns = rng.choice(np.array(WORKLOAD["n_choices"]), size=count)
+    ns = rng.choice(np.array(n_choices or WORKLOAD["n_choices"]), size=count)
     Ls = rng.uniform(*WORKLOAD["L_range"], size=count)
     k = np.arange(1, WORKLOAD["ic_modes"] + 1)
     amps = rng.standard_normal((count, k.size)) * np.exp(-k / 4.0)
@@ -262,6 +262,7 @@ def gpu_arm(args, rank, world, cpu_line):
     eng.events = []
     eng.record_events = True
     launches0 = eng.launches
+    kernels0 = eng.kernel_launches
     mode_steps = 0
     flops = 0.0
     stream = torch.cuda.current_stream(dev)
@@ -284,6 +285,7 @@ def gpu_arm(args, rank, world, cpu_line):
     elapsed = e0.elapsed_time(e1) * 1e-3
     kernel_s = sum(a.elapsed_time(b) for a, b in eng.events) * 1e-3
     n_launch = eng.launches - launches0
+    n_kernels = eng.kernel_launches - kernels0
     status = st["status"]
     max_elapsed = sharding.max_over_ranks(elapsed, dev)
     total_mode_steps = sharding.sum_over_ranks(mode_steps, dev)
@@ -347,11 +349,13 @@ def gpu_arm(args, rank, world, cpu_line):
                            "MEASURED_PEAKS.json carries no FP32 CUDA-core figure)",
             "flops_per_launch": flops / max(n_launch, 1),
             "kernel_ms_per_launch": kernel_s / max(n_launch, 1) * 1e3,
+            "launch": "one rk_evolve call = %d concurrent grid-size-class kernels, timed together" % (
+                n_kernels // max(n_launch, 1)),
         },
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": vec_bytes + state_bytes,
                 "d2h_bytes_per_step": vec_bytes + state_bytes},
-        "gpu_launches": n_launch,
+        "gpu_launches": n_kernels,
         "cpu_baseline": cpu_line,
     }
     print(json.dumps(line), flush=True)
@@ -426,7 +430,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tune-cache", default="", help="JSON file of tuned launch shapes to load, or to write")
+    ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="smaller cases for profiling")
+    ap.add_argument("--sizes", default="", help="comma-separated subset of the grid sizes (profiling)")
+    ap.add_argument("--tf", type=float, default=WORKLOAD["tf"], help="final time (profiling)")
     args = ap.parse_args()
+    WORKLOAD["instances"] = args.instances
+    WORKLOAD["tf"] = args.tf
+    if args.sizes:
+        WORKLOAD["n_choices"] = [int(v) for v in args.sizes.split(",")]
     world = int(os.environ.get("WORLD_SIZE", 1))
     rank = int(os.environ.get("RANK", 0))
     if args.impl == "reference":

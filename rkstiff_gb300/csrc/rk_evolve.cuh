@@ -73,6 +73,47 @@ struct Ctx {
 // ---------------------------------------------------------------------------------
 // built-in nonlinearities: out[j] = N(k)[j] with k[j] = kf(j)
 // ---------------------------------------------------------------------------------
+// Transform part of the built-in nonlinearities for a compile-time grid size, kept out of
+// line so that its fully unrolled passes exist once per kernel rather than once per stage.
+// The packed spectrum is in fa (padded); the result goes to out[0 .. m).
+//
+// u*ux on a real grid: inverse FFT of n points, the product written as reals by the last
+// inverse pass, forward FFT of n/2 points, split into the n/2+1 rfft modes times c.
+template <class T, int LOGN>
+__device__ __noinline__ void uux_core(Group g, cx<T>* fa, cx<T>* fb, const cx<T>* tws, T c,
+                                      cx<T>* __restrict__ out) {
+  constexpr int n = 1 << LOGN, M = n >> 1;
+  // last inverse pass writes the real product u*ux; the forward transform of length n/2
+  // reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
+  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [](cx<T>* y, int idx, cx<T> v) {
+    reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
+  });
+  cx<T>* other = (w == fa) ? fb : fa;
+  cx<T>* F = fft_ct<T, LOGN - 1, false, LOGN>(g, w, other, tws, StoreY<T>());
+  for (int k = g.tid; k <= M; k += g.nthr) {
+    cx<T> Fk = F[fpad(k == M ? 0 : k)];
+    cx<T> Fm = conj(F[fpad(k == 0 ? 0 : M - k)]);
+    cx<T> Fe = (Fk + Fm) * T(0.5);
+    cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+    cx<T> W = Fe + (k == M ? cx<T>{T(-1), T(0)} : tws[fpad(k)]) * Fo;
+    out[k] = W * c;
+  }
+  g.sync();
+}
+
+// i c |v|^2 v on a complex grid: inverse FFT, the pointwise product in the last inverse
+// pass, forward FFT writing the n modes.
+template <class T, int LOGN>
+__device__ __noinline__ void nls_core(Group g, cx<T>* fa, cx<T>* fb, const cx<T>* tws, T c,
+                                      cx<T>* __restrict__ out) {
+  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [c](cx<T>* y, int idx, cx<T> v) {
+    T a2 = (v.x * v.x + v.y * v.y) * c;
+    y[fpad(idx)] = cx<T>{-a2 * v.y, a2 * v.x};
+  });
+  cx<T>* other = (w == fa) ? fb : fa;
+  fft_ct<T, LOGN, false, LOGN>(g, w, other, tws, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
+}
+
 template <class T, class CT, int LOGN, class KF>
 RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
   const Group& g = x.g;
@@ -114,13 +155,8 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     g.sync();
     cx<T>* F;
     if constexpr (LOGN > 0) {
-      // last inverse pass writes the real product u*ux; the forward transform of
-      // length n/2 reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
-      cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, x.fa, x.fb, x.tws, [](cx<T>* y, int idx, cx<T> v) {
-        reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
-      });
-      cx<T>* other = (w == x.fa) ? x.fb : x.fa;
-      F = fft_ct<T, LOGN - 1, false, LOGN>(g, w, other, x.tws, StoreY<T>());
+      uux_core<T, LOGN>(g, x.fa, x.fb, x.tws, x.nl_c, out);
+      return;
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
@@ -136,6 +172,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     // exp(-2 pi i k/n) from the n-point shared table (compile-time path) or the global one
     const cx<T>* twu = LOGN > 0 ? x.tws : x.tw;
     const int tws = LOGN > 0 ? 1 : (RK_TW_N >> x.logn);
+    auto TP = [](int c) { return LOGN > 0 ? fpad(c) : c; };  // the shared table is padded
     for (int k0 = g.tid; k0 <= M; k0 += PK * g.nthr) {
       cx<T> W[PK];
 #pragma unroll
@@ -146,7 +183,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
         cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
         cx<T> Fe = (Fk + Fm) * T(0.5);
         cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[k * tws]) * Fo;
+        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[TP(k * tws)]) * Fo;
       }
 #pragma unroll
       for (int q = 0; q < PK; ++q) {
@@ -177,12 +214,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     g.sync();
     const T c = x.nl_c;
     if constexpr (LOGN > 0) {
-      cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, x.fa, x.fb, x.tws, [c](cx<T>* y, int idx, cx<T> v) {
-        T a2 = (v.x * v.x + v.y * v.y) * c;
-        y[fpad(idx)] = cx<T>{-a2 * v.y, a2 * v.x};
-      });
-      cx<T>* other = (w == x.fa) ? x.fb : x.fa;
-      fft_ct<T, LOGN, false, LOGN>(g, w, other, x.tws, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
+      nls_core<T, LOGN>(g, x.fa, x.fb, x.tws, c, out);
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
@@ -761,7 +793,7 @@ __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const 
   if constexpr (LOGN > 0) {
     tws = reinterpret_cast<cx<T>*>(smem + (size_t)ngroups * group_smem);
     const cx<T>* tw = reinterpret_cast<const cx<T>*>(b.twiddle);
-    for (int j = threadIdx.x; j < (1 << LOGN); j += blockDim.x) tws[j] = tw[j * (RK_TW_N >> LOGN)];
+    for (int j = threadIdx.x; j < (1 << LOGN); j += blockDim.x) tws[fpad(j)] = tw[j * (RK_TW_N >> LOGN)];
     __syncthreads();
   }
   unsigned char* base = smem + (size_t)gi * group_smem;

@@ -222,8 +222,10 @@ RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = x[fpad(i + r * NB)];
     if constexpr (Ls > 1) {
+      // twiddle tables of 2^TWLOG <= 4096 entries live in shared memory at padded
+      // positions (strided reads would otherwise fall into a few banks)
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tw, r * k * TWS);
+      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tw, fpad(r * k * TWS));
     }
     dft_reg<T, R, INV>(v);
     const int j = ((i - k) << LGR) + k;
@@ -249,7 +251,8 @@ RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw,
 }
 
 // FFT of 2^LOGN points held in `a` at padded positions fpad(i) (`b` is scratch of the same
-// size), with `tw` a table of the 2^TWLOG twiddles exp(-2 pi i k/2^TWLOG), TWLOG >= LOGN.
+// size), with `tw` a table of the 2^TWLOG twiddles exp(-2 pi i k/2^TWLOG), TWLOG >= LOGN,
+// stored at padded positions fpad(k).
 // The final pass hands every output to fin(y, index, value), where y is the buffer that
 // pass does not read and `index` the unpadded output index; returns y.  All group threads
 // call.

@@ -166,7 +166,8 @@ class DiagEnsemble:
         self.tw = twiddles(dev, self.prec)
         self.cdtype = complex_dtype(self.prec)
         self.set_config(config, etd_config)
-        self.launches = 0          # rk_evolve launches issued by this ensemble
+        self.launches = 0          # rk_evolve calls issued by this ensemble
+        self.kernel_launches = 0   # evolve-kernel launches (one per non-empty grid-size class)
         self.record_events = False  # when True, (start, end) CUDA events bracket each launch
         self.events = []
 
@@ -271,6 +272,7 @@ class DiagEnsemble:
                 ev1.record(stream)
                 self.events.append((ev0, ev1))
         self.launches += 1
+        self.kernel_launches += int(np.count_nonzero(np.diff(self.class_start)))
 
     def evolve(self, u_dev: torch.Tensor, t0, tf, h, store_freq: int = 0, snap_cap: int = 0,
                max_steps: int = 200_000, max_launches: int = 100_000, on_snapshots=None) -> np.ndarray:
