@@ -183,6 +183,26 @@ int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m
  * (_update_stages) with the built-in nonlinearity fused between in-shared-memory FFTs. */
 int rk_evolve(const rk_batch* b, void* stream);
 
+/* Size of the device scratch array rk_evolve_noalloc places its scratch in: 8 MiB, held by
+ * every GPU that loads the library until the process exits. */
+#define RK_NOALLOC_SCRATCH_BYTES (8u << 20)
+
+/* No counterpart in the reference.  rk_evolve for callers that cannot allocate device
+ * memory -- code running inside another component's CUDA stream capture, plugins whose
+ * host application owns every device allocation, hosts that forbid allocation after
+ * start-up.  Same batch and results as rk_evolve, but the batch's `slab`, `slab_off` and
+ * `queue` fields are ignored: that scratch is carved from one library-owned device array of
+ * RK_NOALLOC_SCRATCH_BYTES (uniform slabs sized for n_max, the offset table and the queue
+ * counters), and all instances run as one launch of the runtime-size kernel (no per-size
+ * class split, so no side streams are created).  Batches that need more scratch are
+ * rejected with RK_E_SIZE.  The call allocates nothing (no cudaMalloc/cudaFree, no stream or
+ * event creation).  The first call on a device looks up the array's device address with
+ * cudaGetSymbolAddress, so make that first call before any stream capture.  Every call
+ * shares the array and it keeps the previous call's contents: the call resets each
+ * instance's cached-coefficient key (state[i].h_coeff = NaN) and the queue counters itself,
+ * and calls whose work overlaps on the GPU (other streams, other host threads) race on it. */
+int rk_evolve_noalloc(const rk_batch* b, void* stream);
+
 /* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
  * each run 8 independent FP32 FMA chains of `iters` steps and write one float to
  * out[blocks*threads] [device].  FLOPs = 16 * blocks * threads * iters; timing it gives the

@@ -69,7 +69,7 @@ assert STATE_DTYPE.itemsize == 128
 
 # every symbol the header declares
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
-           "rk_evolve", "rk_probe_fp32")
+           "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc")
 
 _lib = None
 _lock = threading.Lock()
@@ -104,6 +104,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_evolve.restype = ctypes.c_int
         lib.rk_probe_fp32.argtypes = [vp, i32, i32, i32, vp]
         lib.rk_probe_fp32.restype = ctypes.c_int
+        lib.rk_evolve_noalloc.argtypes = [ctypes.POINTER(RkBatch), vp]
+        lib.rk_evolve_noalloc.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib
