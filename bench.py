@@ -214,6 +214,77 @@ def measure_fp32_peak(device) -> float:
     return best / 1e12
 
 
+FORMS = {"workload": "burgers_ensemble_etd35", "instances": 2048, "n": 512, "nu_range": [1e-3, 1e-1],
+         "epsilon": 1e-5, "tf": 5.0, "seed": 7, "reference_epsilon": 1e-10, "reference_sample": 256}
+
+
+def forms_comparison(dev) -> dict:
+    """Plain FP64, plain FP32 and FP32 + learned controller on the viscous Burgers ensemble
+    (2048 instances the controller was not trained on): mode-steps/s, NL evaluations per
+    unit simulated time, rejected steps, and rel L2 error against an FP64 run at
+    epsilon = 1e-10 on a sample of the instances every form finishes."""
+    import torch
+
+    from rkstiff_gb300 import workloads
+    from rkstiff_gb300.controller import LearnedController
+    from rkstiff_gb300.ensemble import Ensemble
+    from rkstiff_gb300.solveras import SolverConfig
+
+    inst = workloads.burgers_ensemble(FORMS["instances"], FORMS["seed"], n=FORMS["n"], nu_range=FORMS["nu_range"])
+    lins, nls, u0s = [a[0] for a in inst], [a[1] for a in inst], [a[2] for a in inst]
+    ctl = LearnedController.pretrained(device=dev)
+    stream = torch.cuda.current_stream(dev)
+    runs = {}
+    for name, prec, learned in (("plain_fp64", "fp64", False), ("plain_fp32", "fp32", False),
+                                ("learned_fp32", "fp32", True)):
+        ens = Ensemble("ETD35", lins, nls, config=SolverConfig(epsilon=FORMS["epsilon"]), precision=prec, device=dev)
+        if learned:
+            ctl.install(ens)
+        u0 = ens.pack(u0s)
+        u = torch.empty_like(u0)
+        best = None
+        for rep in range(3):  # one warm-up, best of two
+            u.copy_(u0)
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = ens.evolve_packed(u, 0.0, FORMS["tf"], max_steps=20000, max_launches=3)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if rep > 0:
+                dt = e0.elapsed_time(e1) * 1e-3
+                best = dt if best is None else min(best, dt)
+        runs[name] = (st, best, [o.cpu().numpy() for o in ens.engine.unpack_u(u)], ens.engine.ms.copy())
+    ok = np.ones(len(inst), bool)
+    for st, _, _, _ in runs.values():
+        ok &= st["status"] == 0
+    idx = np.where(ok)[0][:: max(1, int(ok.sum()) // FORMS["reference_sample"])][: FORMS["reference_sample"]]
+    ref_ens = Ensemble("ETD35", [lins[i] for i in idx], [nls[i] for i in idx],
+                       config=SolverConfig(epsilon=FORMS["reference_epsilon"]), precision="fp64", device=dev)
+    ref = [o.cpu().numpy() for o in ref_ens.evolve([u0s[i] for i in idx], 0.0, FORMS["tf"], max_steps=50000,
+                                                    max_launches=2)]
+    out = {"config": FORMS, "instances_finished_by_all": int(ok.sum())}
+    for name, (st, dt, finals, ms) in runs.items():
+        errs = np.array([np.linalg.norm(finals[i] - r) / np.linalg.norm(r) for i, r in zip(idx, ref)])
+        out[name] = {
+            "mode_steps_per_s": float(np.sum(ms * st["steps"])) / dt,
+            "seconds": dt,
+            "finished": int(np.sum(st["status"] == 0)),
+            "nl_evals_per_unit_time": float(np.sum(st["nl_evals"][ok])) / (FORMS["tf"] * ok.sum()),
+            "rejects": int(np.sum(st["rejects"][ok])),
+            "accepted_steps": int(np.sum(st["steps"][ok])),
+            "rel_l2_median": float(np.median(errs)),
+            "rel_l2_p90": float(np.quantile(errs, 0.9)),
+        }
+    p64, l32 = out["plain_fp64"], out["learned_fp32"]
+    out["learned_fp32_over_plain_fp64"] = {
+        "mode_steps_per_s": l32["mode_steps_per_s"] / p64["mode_steps_per_s"],
+        "nl_evals_per_unit_time": l32["nl_evals_per_unit_time"] / p64["nl_evals_per_unit_time"],
+    }
+    return out
+
+
 def gpu_arm(args, rank, world, cpu_line):
     import torch
 
@@ -312,6 +383,7 @@ def gpu_arm(args, rank, world, cpu_line):
     if rank != 0:
         return
     peak = measure_fp32_peak(dev)
+    forms = forms_comparison(dev) if (world == 1 and not args.no_forms) else None
     achieved = flops / kernel_s / 1e12
     counts = {name: int(np.sum(status == code)) for name, code in (("done", 0), ("max_loops", 1), ("min_step", 2))}
     line = {
@@ -358,6 +430,8 @@ def gpu_arm(args, rank, world, cpu_line):
         "gpu_launches": n_kernels,
         "cpu_baseline": cpu_line,
     }
+    if forms is not None:
+        line["forms"] = forms
     print(json.dumps(line), flush=True)
 
 
@@ -429,6 +503,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the plain/learned Burgers comparison")
     ap.add_argument("--tune-cache", default="", help="JSON file of tuned launch shapes to load, or to write")
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="smaller cases for profiling")
     ap.add_argument("--sizes", default="", help="comma-separated subset of the grid sizes (profiling)")

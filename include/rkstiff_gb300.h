@@ -144,7 +144,31 @@ typedef struct rk_batch {
   const int32_t* class_threads; /* [host] threads per instance per class (NULL: auto)     */
   const int32_t* class_place;   /* [host] placement per class (NULL: `placement`)         */
   const int32_t* class_groups;  /* [host] instance groups per block per class (NULL: auto) */
+  /* Optional per-attempt log: instance i writes RK_LOG_FIELDS floats per attempt at
+   * attempt_log + (i * log_cap + k) * RK_LOG_FIELDS for its attempts k < log_cap
+   * (counted over the whole evolve).  NULL: no log. */
+  float* attempt_log;
+  int32_t log_cap;
+  /* Learned step-size controller (adaptive methods): after an accepted attempt the next
+   * step is h * exp(y) / mlp_target, y the output of the MLP in `mlp` (RK_MLP_* layout,
+   * bf16 weights), the factor clamped to [0.5, 4]; a rejected attempt keeps the
+   * reference's rule.  NULL: the reference's controller (solveras.py:508-554). */
+  float mlp_target;
+  const void* mlp;
 } rk_batch;
+
+/* per-attempt log record: t, h, s (inf/NaN stored as 1e30 / -1), accepted (0/1), fraction
+ * of |unew|^2 in the top quarter of the modes, rejects so far in the step, grid n, method */
+#define RK_LOG_FIELDS 8
+
+/* learned controller: MLP with RK_MLP_IN inputs, two tanh layers of RK_MLP_H units and one
+ * linear output.  Training parameters (FP32, flat): W1[H][IN], b1[H], W2[H][H], b2[H],
+ * w3[H], b3 -- RK_MLP_NPARAM floats.  Inference buffer (rk_mlp_pack): float mu[IN],
+ * inv_sd[IN], b1[H], b2[H], b3, pad[3], then bf16 W1[H][IN], W2[H][H], w3[H]. */
+#define RK_MLP_IN 8
+#define RK_MLP_H 64
+#define RK_MLP_NPARAM (RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1)
+#define RK_MLP_PACK_BYTES ((2 * RK_MLP_IN + 2 * RK_MLP_H + 4) * 4 + (RK_MLP_H * RK_MLP_IN + RK_MLP_H * RK_MLP_H + RK_MLP_H) * 2)
 
 /* where an instance's scratch arrays live during a launch */
 enum {
@@ -202,6 +226,22 @@ int rk_evolve(const rk_batch* b, void* stream);
  * instance's cached-coefficient key (state[i].h_coeff = NaN) and the queue counters itself,
  * and calls whose work overlaps on the GPU (other streams, other host threads) race on it. */
 int rk_evolve_noalloc(const rk_batch* b, void* stream);
+
+/* Learned step-size controller (no counterpart in the reference).  Training kernels on a
+ * batch of `batch` samples X[batch][RK_MLP_IN] with targets T[batch], FP32:
+ *   rk_mlp_forward: Y[batch] = MLP(params; X)
+ *   rk_mlp_grad:    grad += d/dparams of sum_i (Y_i - T_i)^2 / norm over this batch
+ *                   (caller zeroes grad), *loss += sum_i (Y_i - T_i)^2 / norm
+ *   rk_mlp_adam:    one Adam update of params (m, v moments, step >= 1)
+ *   rk_mlp_pack:    inference buffer (RK_MLP_PACK_BYTES) from params and the feature
+ *                   normalisation mu / sd (RK_MLP_IN each)
+ * All pointers [device]. */
+int rk_mlp_forward(const float* params, const float* X, int64_t batch, float* Y, void* stream);
+int rk_mlp_grad(const float* params, const float* X, const float* T, int64_t batch, float norm, float* grad,
+                float* loss, void* stream);
+int rk_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t step, float lr, float beta1,
+                float beta2, float eps, void* stream);
+int rk_mlp_pack(const float* params, const float* mu, const float* sd, void* out, void* stream);
 
 /* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
  * each run 8 independent FP32 FMA chains of `iters` steps and write one float to

@@ -55,6 +55,8 @@ class RkBatch(ctypes.Structure):
         ("class_n", ctypes.c_void_p), ("class_start", ctypes.c_void_p),
         ("class_threads", ctypes.c_void_p), ("class_place", ctypes.c_void_p),
         ("class_groups", ctypes.c_void_p),
+        ("attempt_log", ctypes.c_void_p), ("log_cap", ctypes.c_int32), ("mlp_target", ctypes.c_float),
+        ("mlp", ctypes.c_void_p),
     ]
 
 
@@ -69,7 +71,12 @@ assert STATE_DTYPE.itemsize == 128
 
 # every symbol the header declares
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
-           "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc")
+           "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
+           "rk_mlp_pack")
+RK_LOG_FIELDS = 8
+RK_MLP_IN, RK_MLP_H = 8, 64
+RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
+RK_MLP_PACK_BYTES = (2 * RK_MLP_IN + 2 * RK_MLP_H + 4) * 4 + (RK_MLP_H * RK_MLP_IN + RK_MLP_H * RK_MLP_H + RK_MLP_H) * 2
 
 _lib = None
 _lock = threading.Lock()
@@ -106,6 +113,13 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_probe_fp32.restype = ctypes.c_int
         lib.rk_evolve_noalloc.argtypes = [ctypes.POINTER(RkBatch), vp]
         lib.rk_evolve_noalloc.restype = ctypes.c_int
+        f32 = ctypes.c_float
+        lib.rk_mlp_forward.argtypes = [vp, vp, i64, vp, vp]
+        lib.rk_mlp_grad.argtypes = [vp, vp, vp, i64, f32, vp, vp, vp]
+        lib.rk_mlp_adam.argtypes = [vp, vp, vp, vp, i64, f32, f32, f32, f32, vp]
+        lib.rk_mlp_pack.argtypes = [vp, vp, vp, vp, vp]
+        for fn in (lib.rk_mlp_forward, lib.rk_mlp_grad, lib.rk_mlp_adam, lib.rk_mlp_pack):
+            fn.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

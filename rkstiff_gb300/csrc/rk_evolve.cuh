@@ -10,6 +10,7 @@
 #include "rk_coeffs.cuh"
 #include "rk_common.cuh"
 #include "rk_fft.cuh"
+#include "rk_mlp.cuh"
 
 namespace rk {
 
@@ -618,6 +619,31 @@ RK_DEV double accept_h(double s, double h, const rk_controller& c) {
   return s > c.incr_f ? s * h : h;
 }
 
+// Fraction of sum |unew|^2 held by the top quarter of the modes (a spectral-resolution
+// feature of the learned controller and of the attempt log).
+template <class T, class CT, int LOGN>
+RK_DEV float tail_fraction(const Ctx<T, CT, LOGN>& x) {
+  df tail{0.f, 0.f}, tot{0.f, 0.f};
+  // the top quarter of |k|: rfft modes j >= 3m/4; a full fft grid (m = n) has |k| >= 3n/8
+  // at indices [3n/8, 5n/8]
+  const bool full = x.m == x.n;
+  const int j0 = full ? (3 * x.n) / 8 : (3 * x.m) / 4;
+  const int j1 = full ? (5 * x.n) / 8 : x.m - 1;
+  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+    const cx<T> v = x.unew[j];
+    const float a2 = (float)(v.x * v.x + v.y * v.y);
+    tot = df_add(tot, a2);
+    if (j >= j0 && j <= j1) tail = df_add(tail, a2);
+  }
+  double st, sa;
+  group_sum2_df(x.g, x.red, tail, tot, st, sa);
+  x.g.sync();
+  return sa > 0.0 ? (float)(st / sa) : 0.f;
+}
+
+RK_DEV float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+RK_DEV float safe_log(double v) { return (v > 0.0 && v < 1e300) ? (float)log(v) : (v > 0.0 ? 690.f : -690.f); }
+
 // ---------------------------------------------------------------------------------
 // one instance, start to pause/finish
 //
@@ -630,7 +656,7 @@ enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
-                         unsigned char* sm_slab, const cx<T>* tws) {
+                         unsigned char* sm_slab, const cx<T>* tws, float* mlp_s) {
   using Tr = Traits<METHOD>;
   Ctx<T, CT, LOGN> x;
   x.g = g;
@@ -676,6 +702,12 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   int64_t attempts = 0, rejects = 0, nl_evals = 0, coeff_updates = 0;
   double s_last = st.s_last, h_used = st.h_used, h_sug = st.h_suggest;
 
+  // learned-controller features and the attempt log
+  const bool learned = Tr::ADAPT && b.mlp != nullptr;
+  const bool want_tail = learned || b.attempt_log != nullptr;
+  float s_prev = 0.f, s_prev2 = 0.f, acc_prev = 1.f, tail_prev = -1.f;  // log s history starts neutral
+  double h_prev = 0.0;
+
   if (b.run_mode == RK_RUN_EVOLVE && !(t < tf)) status = RK_ST_DONE;
   while (status == RK_ST_RUNNING) {
     if (Tr::ADAPT) {
@@ -697,18 +729,68 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
         }
         double s = run_attempt<T, CT, METHOD>(x, h, ctl, nlc);
         nl_evals += nlc;
-        ++attempts;
         s_last = s;
-        if (isinf(s) || isnan(s) || s < 1.0) {
+        const bool ok = !(isinf(s) || isnan(s) || s < 1.0);
+        const float tail = want_tail ? tail_fraction(x) : 0.f;
+        if (b.attempt_log && g.tid == 0) {
+          const int64_t k = st.attempts + attempts;
+          if (k < b.log_cap) {
+            float* rec = b.attempt_log + ((int64_t)inst * b.log_cap + k) * RK_LOG_FIELDS;
+            rec[0] = (float)t;
+            rec[1] = (float)h;
+            rec[2] = isnan(s) ? -1.f : (isinf(s) || s > 1e30 ? 1e30f : (float)s);
+            rec[3] = ok ? 1.f : 0.f;
+            rec[4] = tail;
+            rec[5] = (float)numloops;
+            rec[6] = (float)x.n;
+            rec[7] = (float)METHOD;
+          }
+        }
+        ++attempts;
+        const float f_s = clampf(safe_log(s), -8.f, 8.f);
+        if (!ok) {
           accept = false;
           ++rejects;
+          h_prev = h;
           h = reject_h(s, h, ctl);
           ++numloops;
+          s_prev2 = s_prev;
+          s_prev = f_s;
+          acc_prev = 0.f;
+          tail_prev = tail;
           if (numloops > 50) { status = RK_ST_MAX_LOOPS; break; }
           if (h < ctl.minh) { status = RK_ST_MIN_STEP; break; }
         } else {
           accept = true;
-          hs = accept_h(s, h, ctl);
+          if (learned) {
+            // The MLP estimates a bounded correction y to log s: log s of the next attempt,
+            // rescaled to this h, is taken as log s + clamp(y, -1, 1) and the next step is
+            // h exp(that) / target.  The error test above still judges every attempt.
+            if (g.tid == 0) {
+              float* f = mlp_s;
+              const float lt = log10f(tail + 1e-30f);
+              f[0] = f_s;
+              f[1] = s_prev;
+              f[2] = s_prev2;
+              f[3] = h_prev > 0.0 ? clampf(safe_log(h / h_prev), -3.f, 3.f) : 0.f;
+              f[4] = acc_prev;
+              f[5] = fminf((float)numloops, 5.f);
+              f[6] = clampf(lt, -30.f, 0.f);
+              f[7] = tail_prev >= 0.f ? clampf(lt - log10f(tail_prev + 1e-30f), -10.f, 10.f) : 0.f;
+            }
+            g.sync();
+            const float y = mlp_infer(g, reinterpret_cast<const unsigned char*>(b.mlp), mlp_s, mlp_s + MLP_IN);
+            const float d = fminf(fmaxf(y, -1.f), 1.f);
+            const double fac = fmin(fmax(exp((double)(f_s + d)) / (double)b.mlp_target, 0.5), 4.0);
+            hs = (y == y) ? h * fac : accept_h(s, h, ctl);
+          } else {
+            hs = accept_h(s, h, ctl);
+          }
+          h_prev = h;
+          s_prev2 = s_prev;
+          s_prev = f_s;
+          acc_prev = 1.f;
+          tail_prev = tail;
           break;
         }
       }
@@ -720,6 +802,9 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       h_used = h;
       h_sug = hs;
       h = (t + hs > tf) ? tf - t : hs;
+      // A next step that can no longer advance t (or, from the learned rule, below minh)
+      // would repeat forever; the reference would loop, this ends the instance instead.
+      if (t < tf && (t + h == t || (learned && h < ctl.minh))) status = RK_ST_MIN_STEP;
     } else {
       if (h != hc) {
         compute_coeffs<T, CT, S, METHOD>(x, h, ec);
@@ -742,6 +827,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     }
     ++st.steps;
     ++steps_this;
+    if (status != RK_ST_RUNNING) break;
     if (b.store_freq > 0 && (st.steps % b.store_freq) == 0 && snap < b.snap_cap) {
       cx<T>* su = reinterpret_cast<cx<T>*>(b.snap_u) + (int64_t)b.snap_cap * mo + (int64_t)snap * x.m;
       for (int j = g.tid; j < x.m; j += g.nthr) su[j] = x.u[j];
@@ -801,7 +887,8 @@ __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const 
   cx<T>* fb = fa + fpad_size(nfft);
   double* red = reinterpret_cast<double*>(fb + fpad_size(nfft));
   int* item_s = reinterpret_cast<int*>(red + 64);
-  unsigned char* sm_slab = reinterpret_cast<unsigned char*>(red + 66);
+  float* mlp_s = reinterpret_cast<float*>(red + 66);
+  unsigned char* sm_slab = reinterpret_cast<unsigned char*>(red + 66 + MLP_SCRATCH_FLOATS / 2);
   const Group g{(int)(threadIdx.x % gthreads), gthreads, gthreads == 32 ? -1 : (ngroups == 1 ? 0 : 1 + gi)};
   for (;;) {
     if (g.tid == 0) *item_s = atomicAdd(queue, 1);
@@ -810,7 +897,7 @@ __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const 
     g.sync();
     if (item >= count) break;
     const int inst = order ? order[item] : item;
-    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws);
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s);
   }
 }
 
@@ -839,7 +926,7 @@ inline size_t smem_slab_bytes(int place, int64_t m) {
 
 // smem bytes of the evolve kernel's FFT buffers and scratch for complex FFT length nfft
 template <class T> inline size_t evolve_smem(int nfft) {
-  return 2 * (size_t)fpad_size(nfft) * sizeof(cx<T>) + 66 * sizeof(double);
+  return 2 * (size_t)fpad_size(nfft) * sizeof(cx<T>) + (66 + MLP_SCRATCH_FLOATS / 2) * sizeof(double);
 }
 
 }  // namespace rk

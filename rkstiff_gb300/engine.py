@@ -170,6 +170,10 @@ class DiagEnsemble:
         self.kernel_launches = 0   # evolve-kernel launches (one per non-empty grid-size class)
         self.record_events = False  # when True, (start, end) CUDA events bracket each launch
         self.events = []
+        self.attempt_log = None     # float32 device tensor [n_inst, log_cap, RK_LOG_FIELDS] or None
+        self.log_cap = 0
+        self.mlp = None             # packed learned-controller buffer (uint8 device tensor) or None
+        self.mlp_target = 1.25
 
     # -- configuration ----------------------------------------------------------------
     def set_config(self, config=None, etd_config=None):
@@ -261,6 +265,10 @@ class DiagEnsemble:
         b.class_threads = self.class_threads.ctypes.data if self.class_threads is not None else None
         b.class_place = self.class_place.ctypes.data if self.class_place is not None else None
         b.class_groups = self.class_groups.ctypes.data if self.class_groups is not None else None
+        b.attempt_log = self.attempt_log.data_ptr() if self.attempt_log is not None else None
+        b.log_cap = int(self.log_cap) if self.attempt_log is not None else 0
+        b.mlp = self.mlp.data_ptr() if self.mlp is not None else None
+        b.mlp_target = float(self.mlp_target)
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
             if self.record_events:
@@ -275,7 +283,7 @@ class DiagEnsemble:
         self.kernel_launches += int(np.count_nonzero(np.diff(self.class_start)))
 
     def evolve(self, u_dev: torch.Tensor, t0, tf, h, store_freq: int = 0, snap_cap: int = 0,
-               max_steps: int = 200_000, max_launches: int = 100_000, on_snapshots=None) -> np.ndarray:
+               max_steps: int = 200_000, max_launches: int = 50, on_snapshots=None) -> np.ndarray:
         """Run every instance from (t0, h) to tf, relaunching while any instance paused
         (full snapshot buffer, or the per-launch bound of ``max_steps`` accepted steps,
         which keeps every launch finite).  ``on_snapshots(state, snap_u, snap_t)``
@@ -300,7 +308,17 @@ class DiagEnsemble:
             st["snap_count"] = 0
             st["status"] = np.where(resume, nat.RK_ST_RUNNING, st["status"])
             self.put_state(st)
-        raise RuntimeError(f"evolve did not reach tf within {max_launches} launches of {max_steps} steps")
+        raise EvolveBoundError(f"evolve did not reach tf within {max_launches} launches of {max_steps} steps",
+                               self.get_state())
+
+
+class EvolveBoundError(RuntimeError):
+    """An evolve stopped by its launch bound; ``state`` holds the records reached so far
+    (paused instances carry RK_ST_ITER_CAP or RK_ST_SNAP_FULL)."""
+
+    def __init__(self, msg: str, state: np.ndarray):
+        super().__init__(msg)
+        self.state = state
 
 
 def snapshot_views(ens: DiagEnsemble, st: np.ndarray, snap_u: torch.Tensor, snap_t: torch.Tensor, inst: int):

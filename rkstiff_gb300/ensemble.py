@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .engine import DiagEnsemble
+from .engine import DiagEnsemble, EvolveBoundError
 from .models import BuiltinNL
 
 STATUS_NAMES = {nat.RK_ST_DONE: "done", nat.RK_ST_MAX_LOOPS: "max_loops", nat.RK_ST_MIN_STEP: "min_step",
@@ -74,7 +74,7 @@ class Ensemble:
         return self.engine.pack_u(u0s)
 
     def evolve_packed(self, u_dev: torch.Tensor, t0: float, tf: float, h_init: Optional[float] = None,
-                      max_steps: int = 200_000) -> np.ndarray:
+                      max_steps: int = 200_000, max_launches: int = 50) -> np.ndarray:
         """Advance the packed state in place from t0 to tf; returns the state records.
 
         ``h_init`` defaults to (tf - t0)/100 and is clamped to the span, as the
@@ -88,13 +88,18 @@ class Ensemble:
             h = tf - t0
         if not self.adaptive and t0 + h > tf:
             raise ValueError("Step size h must be <= (tf - t0); reduce h or extend tf.")
-        self.state = self.engine.evolve(u_dev, t0, tf, h, max_steps=max_steps)
+        try:
+            self.state = self.engine.evolve(u_dev, t0, tf, h, max_steps=max_steps, max_launches=max_launches)
+        except EvolveBoundError as ex:
+            self.state = ex.state
+            raise
         return self.state
 
-    def evolve(self, u0s: Sequence, t0: float, tf: float, h_init: Optional[float] = None):
-        """Evolve all instances; returns the list of final spectra (device tensors)."""
+    def evolve(self, u0s: Sequence, t0: float, tf: float, h_init: Optional[float] = None, **bounds):
+        """Evolve all instances; returns the list of final spectra (device tensors).
+        ``max_steps`` (accepted steps per launch) and ``max_launches`` bound the run."""
         u = self.pack(u0s)
-        self.evolve_packed(u, t0, tf, h_init)
+        self.evolve_packed(u, t0, tf, h_init, **bounds)
         return self.engine.unpack_u(u)
 
     def stats(self) -> dict:
