@@ -45,7 +45,9 @@ enum {
   RK_NL_UUX = 1,  /* N(u) = c rfft(irfft(u) * irfft(i kx u)) on a real grid:
                      KS (README.md:94-97, c=-1), Burgers (models.py:189-192, c=-1),
                      KdV (models.py:140-143, c=-6)                                    */
-  RK_NL_NLS = 2   /* N(u) = fft(i c |v|^2 v), v = ifft(u), on a complex grid (c=1)    */
+  RK_NL_NLS = 2,  /* N(u) = fft(i c |v|^2 v), v = ifft(u), on a complex grid (c=1)    */
+  RK_NL_ALLEN_CAHN = 3 /* dense path: N(w) = x - (w + x)^3 on the interior Chebyshev points
+                          x (models.py:242-244, the lifted form u = w + x)            */
 };
 
 enum { RK_RUN_EVOLVE = 0, RK_RUN_STEP = 1 };
@@ -242,6 +244,59 @@ int rk_mlp_grad(const float* params, const float* X, const float* T, int64_t bat
 int rk_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t step, float lr, float beta1,
                 float beta2, float eps, void* stream);
 int rk_mlp_pack(const float* params, const float* mu, const float* sd, void* out, void* stream);
+
+/* Dense (non-diagonal) lin_op path: ETD35 for a batch of n_inst instances sharing one
+ * operator lin_op (n x n, n <= RK_DENSE_NMAX) with real eigenvalues, lin_op = S diag(eig)
+ * S^-1.  Replaces rkstiff/etd35.py:_Etd35NonDiagonal (etd35.py:498-720) for the
+ * Allen-Cahn Chebyshev operator of models.py:202-247.  The coefficient matrices (the
+ * psi-matrices of etd35.py:602-658) are formed in FP64 on the device whenever h changes,
+ * as S diag(c(h eig)) S^-1 with the diagonal ETD35 coefficient functions (the arithmetic of
+ * the reference's diagonalized form, etd35.py:348-495); the stages run as 3xTF32 tensor-core
+ * GEMMs with FP32 accumulation, one K-concatenated GEMM per stage.
+ * The batch steps in lockstep: one h for every instance, an attempt is accepted when every
+ * instance passes the reference's error test (the smallest s of the batch decides), so a
+ * batch of one instance follows the reference's controller exactly. */
+#define RK_DENSE_NMAX 128
+#define RK_DENSE_TILE 64 /* instances per CTA */
+
+typedef struct rk_dense_state {
+  double t, tf, h, h_coeff, h_suggest, s_last; /* h_coeff: h of the current matrices (NaN: none) */
+  int32_t status;                              /* RK_ST_*                                        */
+  int32_t cur;                                 /* internal: current state buffer                 */
+  int32_t numloops, accept, need_matrix, error; /* error != 0: a device wait timed out            */
+  int32_t n1_fresh, reserved_i;                /* internal: N1 is re-evaluated this attempt      */
+  int64_t steps, attempts, rejects, nl_evals, coeff_updates, reserved;
+} rk_dense_state; /* 128 bytes */
+
+typedef struct rk_dense_batch {
+  int32_t method;        /* RK_ETD35                                                      */
+  int32_t n;             /* vector length, 1..RK_DENSE_NMAX                               */
+  int64_t n_inst;        /* instances                                                     */
+  int32_t nl_kind;       /* RK_NL_ALLEN_CAHN                                              */
+  int32_t reserved0;
+  const double* eig;     /* [device] n real eigenvalues of lin_op                        */
+  const double* S;       /* [device] n x n eigenvectors, row-major                       */
+  const double* Sinv;    /* [device] n x n inverse of S, row-major                       */
+  const double* shift;   /* [device] n points x of the nonlinearity                      */
+  float* u;              /* [device] n_inst x n states, instance-major; in/out            */
+  void* work;            /* [device] rk_dense_work_bytes(n_inst) bytes, 1024-byte aligned */
+  rk_dense_state* state; /* [device] one record; the caller sets t, tf, h, h_coeff = NaN,
+                            status = RK_ST_RUNNING, cur = 0 and zero counters before the
+                            first call                                                   */
+  rk_controller ctl;
+  rk_etd_config etd;
+  int64_t max_attempts;  /* attempts this call may run before returning                   */
+} rk_dense_batch;
+
+int64_t rk_dense_work_bytes(int64_t n_inst);
+/* Runs attempts until the state leaves RK_ST_RUNNING or max_attempts attempts ran; returns
+ * after the stream has completed them (u holds the current states). */
+int rk_dense_evolve(const rk_dense_batch* b, void* stream);
+/* The 3xTF32 tensor-core product of the dense path on its own (no counterpart in the
+ * reference; a check of the GEMM): D[N][128] = B[N][K] * A[128][K]^T, FP32, K a multiple of
+ * 32, N a multiple of RK_DENSE_TILE; work holds rk_tf32x3_work_bytes(K, N) bytes. */
+int64_t rk_tf32x3_work_bytes(int64_t K, int64_t N);
+int rk_tf32x3_gemm(const float* A, const float* B, float* D, int64_t K, int64_t N, void* work, void* stream);
 
 /* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
  * each run 8 independent FP32 FMA chains of `iters` steps and write one float to

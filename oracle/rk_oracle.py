@@ -266,6 +266,24 @@ def _dense_contour_psis(z: Array, cfg: ETDConfig, scales: Tuple[Tuple[int, int],
     return out
 
 
+def dense_coeffs_eig(method: str, lin_op: Array, h: float, cfg: Optional[ETDConfig] = None) -> Dict[str, Array]:
+    """The coefficient matrices of a non-diagonal solver formed through the eigenbasis,
+    M = S diag(c(h lambda)) S^-1 with the diagonal coefficient functions c (diag_coeffs);
+    real when lin_op and its spectrum are real.  Same matrices as dense_coeffs (etd35.py:
+    602-658) wherever the reference's contour mean converges, which it does not for
+    eigenvalues of h lin_op far outside the contour radius; the dense tensor-core path forms
+    its matrices this way."""
+    w, S = np.linalg.eig(lin_op)
+    Sinv = np.linalg.inv(S)
+    C = diag_coeffs(method, w, h, cfg)
+    real = not np.iscomplexobj(lin_op) and np.max(np.abs(np.imag(w))) == 0.0
+    out = {}
+    for k, c in C.items():
+        M = (S * c[None, :]) @ Sinv
+        out[k] = M.real if real else M
+    return out
+
+
 def dense_coeffs(method: str, lin_op: Array, h: float, cfg: Optional[ETDConfig] = None) -> Dict[str, Array]:
     """Coefficient matrices of a non-diagonal solver (etd35.py:602-658, etd34.py:356-392,
     if34.py:225-229, etd4.py:235-271, if4.py:152-164)."""
@@ -491,15 +509,20 @@ class OracleSolver:
     """One rkstiff solver object restated: method + operator + nonlinear map + state.
 
     ``diagonalize`` selects the eigenbasis form (etd35.py:348-495, etd34.py:194-304,
-    if34.py:137-196) for a 2-D operator; otherwise a 2-D operator uses the dense form.
+    if34.py:137-196) for a 2-D operator; otherwise a 2-D operator uses the dense form, whose
+    coefficient matrices come from the reference's contour mean (``dense_psi="contour"``) or
+    from the eigenbasis (``dense_psi="eig"``, see dense_coeffs_eig).
     ``log`` collects one record per attempt: (t, h, s, accepted).
     """
 
     def __init__(self, method: str, lin_op: Array, nl_func: Callable[[Array], Array],
                  config: Optional[SolverConfig] = None, etd_config: Optional[ETDConfig] = None,
-                 diagonalize: bool = False):
+                 diagonalize: bool = False, dense_psi: str = "contour"):
         if method not in METHODS:
             raise ValueError(method)
+        if dense_psi not in ("contour", "eig"):
+            raise ValueError(dense_psi)
+        self.dense_psi = dense_psi
         self.method = method
         self.lin_op = lin_op
         self.nl_func = nl_func
@@ -548,6 +571,8 @@ class OracleSolver:
             self._C = diag_coeffs(self.method, self.lin_op, h, self.etd_config)
         elif self.diagonalize:
             self._C = diag_coeffs(self.method, self._eig, h, self.etd_config)
+        elif self.dense_psi == "eig":
+            self._C = dense_coeffs_eig(self.method, self.lin_op, h, self.etd_config)
         else:
             self._C = dense_coeffs(self.method, self.lin_op, h, self.etd_config)
 

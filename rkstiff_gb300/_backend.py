@@ -80,3 +80,88 @@ class DiagBackend:
     def counters(self):
         st = self.st
         return {k: int(st[k][0]) for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates")}
+
+
+class DenseBackend:
+    """One-instance dense ensemble (rkstiff_gb300.dense) behind a solver object with a 2-D
+    lin_op: ETD35 with FP64 psi-matrices and 3xTF32 tensor-core stages, FP32 states.  With a
+    single instance the lockstep controller is the reference's controller."""
+
+    def __init__(self, solver, method: str):
+        from .dense import DenseEnsemble
+
+        if method != "ETD35":
+            raise NotImplementedError(f"{method}: the dense (2-D lin_op) path implements ETD35")
+        opts = solver.device_options
+        self.solver = solver
+        self.ens = DenseEnsemble(solver.lin_op, solver.nl_func, 1, config=getattr(solver, "config", None),
+                                 etd_config=getattr(solver, "etd_config", None), device=opts.device)
+        self.reset()
+
+    def reset(self):
+        self.st = {"accept": np.zeros(1, np.int32), "h_used": np.zeros(1), "h_suggest": np.zeros(1),
+                   "steps": np.zeros(1, np.int64), "attempts": np.zeros(1, np.int64), "rejects": np.zeros(1, np.int64),
+                   "nl_evals": np.zeros(1, np.int64), "coeff_updates": np.zeros(1, np.int64)}
+        self._dstate = None
+
+    def _sync_config(self):
+        self.ens.config = getattr(self.solver, "config", None) or self.ens.config
+        self.ens.etd_config = getattr(self.solver, "etd_config", None) or self.ens.etd_config
+
+    def _record(self, dst, h_used):
+        for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates", "accept"):
+            self.st[k][0] = dst[k][0]
+        self.st["h_used"][0] = h_used
+        self.st["h_suggest"][0] = dst["h_suggest"][0]
+
+    @staticmethod
+    def _out(u_dev, like):
+        v = u_dev[0].detach()
+        if isinstance(like, torch.Tensor):
+            return v.clone()
+        return v.cpu().numpy().astype(np.float64).astype(np.complex128)
+
+    def evolve(self, u, t0, tf, h, store_data, store_freq):
+        self._sync_config()
+        s = self.solver
+        ens = self.ens
+        u_dev = ens.pack_u(np.asarray(u)[None, :] if not isinstance(u, torch.Tensor) else u.reshape(1, -1))
+        if store_data and int(store_freq) <= 0:
+            raise ValueError("store_freq must be a positive integer")
+        st = ens.fresh_state(t0, tf, h)
+        ens.put_state(st)
+        if not store_data:
+            dst = ens.run(u_dev, 10_000_000)
+        else:
+            freq = int(store_freq)
+            steps = 0
+            while True:
+                dst = ens.run(u_dev, 1)
+                if int(dst["steps"][0]) > steps:
+                    steps = int(dst["steps"][0])
+                    if steps % freq == 0:
+                        s.t.append(float(dst["t"][0]))
+                        s.u.append(self._out(u_dev, u))
+                if int(dst["status"][0]) != nat.RK_ST_RUNNING:
+                    break
+        self._dstate = dst
+        self._record(dst, 0.0)
+        return self._out(u_dev, u), int(dst["status"][0])
+
+    def step(self, u, h):
+        """One accepted step with retries (solveras.py:379-410)."""
+        self._sync_config()
+        ens = self.ens
+        u_dev = ens.pack_u(np.asarray(u)[None, :] if not isinstance(u, torch.Tensor) else u.reshape(1, -1))
+        ens.put_state(ens.fresh_state(0.0, np.inf, h))
+        while True:
+            dst = ens.run(u_dev, 1)
+            if int(dst["steps"][0]) >= 1 or int(dst["status"][0]) != nat.RK_ST_RUNNING:
+                break
+        self._dstate = dst
+        self._record(dst, float(dst["t"][0]))  # t started at 0
+        return self._out(u_dev, u), int(dst["status"][0])
+
+    @property
+    def counters(self):
+        return {k: int(self.st[k][0]) for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates")}

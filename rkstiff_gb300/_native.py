@@ -19,7 +19,7 @@ RK_IF34, RK_ETD35, RK_ETD34, RK_IF45DP, RK_ETD4, RK_ETD5, RK_IF4 = range(7)
 METHOD_IDS = {"IF34": RK_IF34, "ETD35": RK_ETD35, "ETD34": RK_ETD34, "IF45DP": RK_IF45DP,
               "ETD4": RK_ETD4, "ETD5": RK_ETD5, "IF4": RK_IF4}
 RK_FP64, RK_FP32 = 0, 1
-RK_NL_NONE, RK_NL_UUX, RK_NL_NLS = 0, 1, 2
+RK_NL_NONE, RK_NL_UUX, RK_NL_NLS, RK_NL_ALLEN_CAHN = 0, 1, 2, 3
 RK_RUN_EVOLVE, RK_RUN_STEP = 0, 1
 RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
 RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE = 4, 5, 6
@@ -60,6 +60,27 @@ class RkBatch(ctypes.Structure):
     ]
 
 
+class RkDenseBatch(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32), ("n", ctypes.c_int32), ("n_inst", ctypes.c_int64),
+        ("nl_kind", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("eig", ctypes.c_void_p), ("S", ctypes.c_void_p), ("Sinv", ctypes.c_void_p), ("shift", ctypes.c_void_p),
+        ("u", ctypes.c_void_p), ("work", ctypes.c_void_p), ("state", ctypes.c_void_p),
+        ("ctl", RkController), ("etd", RkEtdConfig), ("max_attempts", ctypes.c_int64),
+    ]
+
+
+RK_DENSE_NMAX, RK_DENSE_TILE = 128, 64
+# rk_dense_state (128 bytes)
+DENSE_STATE_DTYPE = np.dtype([
+    ("t", "f8"), ("tf", "f8"), ("h", "f8"), ("h_coeff", "f8"), ("h_suggest", "f8"), ("s_last", "f8"),
+    ("status", "i4"), ("cur", "i4"), ("numloops", "i4"), ("accept", "i4"), ("need_matrix", "i4"), ("error", "i4"),
+    ("n1_fresh", "i4"), ("reserved_i", "i4"),
+    ("steps", "i8"), ("attempts", "i8"), ("rejects", "i8"), ("nl_evals", "i8"), ("coeff_updates", "i8"),
+    ("reserved", "i8"),
+])
+assert DENSE_STATE_DTYPE.itemsize == 128
+
 # rk_inst_state as a NumPy record (128 bytes)
 STATE_DTYPE = np.dtype([
     ("t", "f8"), ("tf", "f8"), ("h", "f8"), ("h_coeff", "f8"), ("h_used", "f8"), ("h_suggest", "f8"),
@@ -72,7 +93,7 @@ assert STATE_DTYPE.itemsize == 128
 # every symbol the header declares
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
-           "rk_mlp_pack")
+           "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -120,6 +141,14 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_mlp_pack.argtypes = [vp, vp, vp, vp, vp]
         for fn in (lib.rk_mlp_forward, lib.rk_mlp_grad, lib.rk_mlp_adam, lib.rk_mlp_pack):
             fn.restype = ctypes.c_int
+        lib.rk_dense_work_bytes.argtypes = [i64]
+        lib.rk_dense_work_bytes.restype = i64
+        lib.rk_dense_evolve.argtypes = [ctypes.POINTER(RkDenseBatch), vp]
+        lib.rk_dense_evolve.restype = ctypes.c_int
+        lib.rk_tf32x3_work_bytes.argtypes = [i64, i64]
+        lib.rk_tf32x3_work_bytes.restype = i64
+        lib.rk_tf32x3_gemm.argtypes = [vp, vp, vp, i64, i64, vp, vp]
+        lib.rk_tf32x3_gemm.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

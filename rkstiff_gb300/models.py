@@ -21,15 +21,19 @@ class BuiltinNL:
 
     kind  : RK_NL_UUX  -> c * rfft(irfft(u) * irfft(i kx u))   (real grid, n points)
             RK_NL_NLS  -> fft(i c |ifft(u)|^2 ifft(u))          (complex grid, n points)
+            RK_NL_ALLEN_CAHN -> x - (u + x)^3 on the points x     (dense operators)
             RK_NL_NONE -> 0
     """
 
-    def __init__(self, kind: int, coef: float, n: int, kx: Optional[np.ndarray] = None, name: str = ""):
+    def __init__(self, kind: int, coef: float, n: int, kx: Optional[np.ndarray] = None, name: str = "",
+                 shift: Optional[np.ndarray] = None):
         self.kind = int(kind)
         self.coef = float(coef)
         self.n = int(n)
         self.kx = None if kx is None else np.asarray(kx, dtype=np.float64)
-        self.name = name or {nat.RK_NL_UUX: "uux", nat.RK_NL_NLS: "nls", nat.RK_NL_NONE: "zero"}[self.kind]
+        self.shift = None if shift is None else np.asarray(shift, dtype=np.float64)
+        self.name = name or {nat.RK_NL_UUX: "uux", nat.RK_NL_NLS: "nls", nat.RK_NL_NONE: "zero",
+                             nat.RK_NL_ALLEN_CAHN: "allen_cahn"}[self.kind]
         self._kx_t = {}
 
     @property
@@ -52,6 +56,9 @@ class BuiltinNL:
         if self.kind == nat.RK_NL_NLS:
             v = torch.fft.ifft(u)
             return torch.fft.fft(1j * self.coef * (v.abs() ** 2) * v)
+        if self.kind == nat.RK_NL_ALLEN_CAHN:
+            x = torch.as_tensor(self.shift, dtype=u.real.dtype if u.is_complex() else u.dtype, device=u.device)
+            return (x - (u + x) ** 3).to(u.dtype)
         return torch.zeros_like(u)
 
     def __call__(self, u):
@@ -62,6 +69,17 @@ class BuiltinNL:
 
     def __repr__(self):
         return f"BuiltinNL({self.name}, coef={self.coef}, n={self.n})"
+
+
+def allen_cahn_ops(x: np.ndarray, d_cheb_matrix: np.ndarray, epsilon: float = 0.01) -> Tuple[np.ndarray, BuiltinNL]:
+    """Allen-Cahn on Chebyshev points (rkstiff/models.py:202-247): L = epsilon D^2 + I without
+    the boundary rows and columns, N(w) = x - (w + x)^3 on the interior points (the state w is
+    u - x, which vanishes at both ends for u(+-1) = +-1)."""
+    x = np.asarray(x, dtype=np.float64)
+    D = np.asarray(d_cheb_matrix, dtype=np.float64)
+    lin = (epsilon * D.dot(D) + np.eye(*D.shape))[1:-1, 1:-1]
+    xi = x[1:-1]
+    return lin, BuiltinNL(nat.RK_NL_ALLEN_CAHN, 1.0, len(xi), None, "allen_cahn", shift=xi)
 
 
 def _n_from_rfft_kx(kx) -> int:

@@ -126,10 +126,11 @@ class BaseSolverAS(BaseSolver):
 
     def _engine(self):
         if self._backend is None:
-            from ._backend import DiagBackend
-            if not self._diag:
-                raise NotImplementedError(f"{type(self).__name__}: a 2-D operator needs the dense path")
-            self._backend = DiagBackend(self, self._method_name)
+            from ._backend import DenseBackend, DiagBackend
+            if self._diag:
+                self._backend = DiagBackend(self, self._method_name)
+            else:
+                self._backend = DenseBackend(self, self._method_name)
         return self._backend
 
     def reset(self) -> None:

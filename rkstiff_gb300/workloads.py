@@ -68,3 +68,31 @@ def ks_ensemble(count: int, seed: int, n_choices: Sequence[int] = (256, 512, 102
         u = np.sum(a[:, None] * np.cos(2 * np.pi * k[:, None] * x[None, :] / L + ph[:, None]), axis=0)
         out.append((lin, nl, np.fft.rfft(u)))
     return out
+
+
+def cheb_points_matrix(n: int, a: float = -1.0, b: float = 1.0):
+    """n + 1 Chebyshev extreme points on [a, b] and the differentiation matrix
+    (rkstiff/grids.py:134-219)."""
+    x = np.polynomial.chebyshev.chebpts2(n + 1)
+    x = a + (b - a) * (x + 1) / 2.0
+    c = np.r_[2, np.ones(n - 1), 2] * np.power(-1, np.arange(0, n + 1))
+    X = np.tile(x.reshape(n + 1, 1), (1, n + 1))
+    dX = X - X.T
+    D = np.outer(c, 1.0 / c) / (dX + np.eye(n + 1))
+    return x, D - np.diag(D.sum(axis=1))
+
+
+def allen_cahn_batch(count: int, seed: int, n: int = 129, epsilon: float = 0.01):
+    """Allen-Cahn on the n + 1 Chebyshev points of [-1, 1] (n - 1 interior points, 128 for
+    n = 129) with u(+-1) = +-1: (lin_op, nl_func, w0[count, n-1]) where
+    u0 = 0.53 x + 0.47 sin(-1.5 pi x) + 0.1 N(0, 1) smoothed by a 5-point moving average on
+    the interior, and w0 = u0 - x (the lifted state of models.allen_cahn_ops)."""
+    x, D = cheb_points_matrix(n)
+    lin, nl = models.allen_cahn_ops(x, D, epsilon)
+    xi = x[1:-1]
+    rng = np.random.default_rng(seed)
+    base = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi)
+    noise = 0.1 * rng.standard_normal((count, xi.size))
+    k = np.ones(5) / 5.0
+    smooth = np.stack([np.convolve(r, k, mode="same") for r in noise])
+    return lin, nl, base[None, :] + smooth - xi[None, :]

@@ -90,3 +90,31 @@ def test_struct_layout_matches_c():
     soffs = vals[4 + len(fields):]
     for f, o in zip(nat.STATE_DTYPE.names, soffs):
         assert nat.STATE_DTYPE.fields[f][1] == o, f
+
+
+def test_dense_struct_layout_matches_c():
+    """rk_dense_batch / rk_dense_state offsets from the header against the ctypes / NumPy views."""
+    fields = [f for f, _ in nat.RkDenseBatch._fields_]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){",
+             'printf("%zu %zu\\n", sizeof(rk_dense_batch), sizeof(rk_dense_state));']
+    for f in fields:
+        lines.append(f'printf("%zu\\n", offsetof(rk_dense_batch, {f}));')
+    for f in nat.DENSE_STATE_DTYPE.names:
+        lines.append(f'printf("%zu\\n", offsetof(rk_dense_state, {f}));')
+    lines.append('printf("%d %d %d\\n", RK_DENSE_NMAX, RK_DENSE_TILE, RK_NL_ALLEN_CAHN);')
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        exe = os.path.join(d, "probe")
+        open(c, "w").write("\n".join(lines))
+        subprocess.run(["gcc", "-O0", c, "-o", exe], check=True)
+        vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(nat.RkDenseBatch)
+    assert vals[1] == nat.DENSE_STATE_DTYPE.itemsize == 128
+    offs = vals[2:2 + len(fields)]
+    for f, o in zip(fields, offs):
+        assert getattr(nat.RkDenseBatch, f).offset == o, f
+    soffs = vals[2 + len(fields):2 + len(fields) + len(nat.DENSE_STATE_DTYPE.names)]
+    for f, o in zip(nat.DENSE_STATE_DTYPE.names, soffs):
+        assert nat.DENSE_STATE_DTYPE.fields[f][1] == o, f
+    assert vals[-3:] == [nat.RK_DENSE_NMAX, nat.RK_DENSE_TILE, nat.RK_NL_ALLEN_CAHN]

@@ -204,3 +204,48 @@ def test_dense_allen_cahn(golden):
     assert _close(s.evolve(w0, 0, 2, 0.01, store_data=False), g["ac20_IF4_dense_final"], 1e-12)
     s = O.OracleSolver("ETD4", g["ac20_lin"], nl, etd_config=cfg)
     assert _close(s.evolve(w0, 0, 2, 0.01, store_data=False), g["ac20_ETD4_dense_final"], 1e-12)
+
+
+def _augmented_phis(Z):
+    """phi_1..3(Z) from the exponential of the block matrix [[Z, I, 0, 0], [0, 0, I, 0],
+    [0, 0, 0, I], [0, 0, 0, 0]] (its top row holds e^Z, phi_1, phi_2, phi_3)."""
+    import scipy.linalg as sl
+
+    n = Z.shape[0]
+    A = np.zeros((4 * n, 4 * n))
+    A[:n, :n] = Z
+    for k in range(3):
+        A[k * n:(k + 1) * n, (k + 1) * n:(k + 2) * n] = np.eye(n)
+    E = sl.expm(A)
+    return E[:n, n:2 * n], E[:n, 2 * n:3 * n], E[:n, 3 * n:]
+
+
+def test_dense_coeffs_eig_matches_augmented_expm(golden):
+    """The eigenbasis psi-matrices the dense tensor-core path uses, against an independent
+    FP64 method, for every ETD35 coefficient of the reference's n=20 Allen-Cahn operator."""
+    lin = golden("dense")["ac20_lin"]
+    for h in (0.05, 0.4):
+        C = O.dense_coeffs_eig("ETD35", lin, h)
+        ph = {c: _augmented_phis(c * h * lin) for c in (0.25, 0.5, 0.75, 1.0)}
+        p = {c: (ph[c][0], 2 * ph[c][1], 6 * ph[c][2]) for c in ph}  # psi_k = k! phi_k
+        ref = {
+            "a21": h * p[0.25][0] / 4.0, "a32": h * p[0.25][1] / 8.0, "a43": h * p[0.5][1] / 2.0,
+            "a54": h * 9 * p[0.75][1] / 16.0, "a62": h * 8 * p[1.0][0] / 7.0,
+            "a65": h * (-47 * p[1.0][0] + 143 * p[1.0][1]) / 84.0,
+            "a76": h * (509 * p[1.0][0] - 2129 * p[1.0][1] + 1830 * p[1.0][2]) / 2700,
+        }
+        for k, v in ref.items():
+            assert _close(C[k], v, 1e-9), (h, k)
+        import scipy.linalg as sl
+        assert _close(C["E"], sl.expm(h * lin), 1e-12)
+
+
+def test_dense_coeffs_eig_vs_reference_contour_arrays(golden):
+    """Against the reference's own dense arrays (contour radius 10, 32 points, h=0.05): they
+    agree to the contour's truncation error (the trapezoidal rule's aliasing term is of
+    order R^32/32! for these entire functions, about 1e-5 at R=10)."""
+    g = golden("dense")
+    C = O.dense_coeffs_eig("ETD35", g["ac20_lin"], 0.05)
+    for name in ("a21", "a54", "a65", "a76"):
+        assert _close(C[name], g[f"ac20_ETD35_dense_{name}"], 3e-5), name
+    assert _close(C["E"], g["ac20_ETD35_dense_EL"], 1e-13)
