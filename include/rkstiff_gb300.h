@@ -229,6 +229,28 @@ int rk_evolve(const rk_batch* b, void* stream);
  * and calls whose work overlaps on the GPU (other streams, other host threads) race on it. */
 int rk_evolve_noalloc(const rk_batch* b, void* stream);
 
+/* Stepping with a user-supplied nonlinearity.  The reference accepts any callable nl_func
+ * (solver.py:104-115); this build evaluates such a callable on the device between two
+ * kernels of its own:
+ *   rk_combine: out[j] = sum_i w_i * coef_i[j] * v_i[j] (coef_i NULL: w_i * v_i[j]) for 1..8
+ *               terms - the stage combinations of the _update_stages methods
+ *               (etd35.py:320-345, etd34.py:182-190, if34.py:120-130, if45dp.py:140-179,
+ *               etd4.py:167-174, etd5.py:236-260, if4.py:112-121) as one pass; vectors
+ *               complex (complex128 / complex64 per precision), coefficients real or
+ *               complex per coef_complex in the same precision
+ *   rk_error_s: *s_out = safety (eps |u[mask]| / |err[mask]|)^(1/q), the mask and norms of
+ *               solveras.py:412-455, in FP64 on the device
+ * All pointers [device] except terms (host array) and ctl (host). */
+typedef struct rk_term {
+  const void* coef;
+  const void* v;
+  double w;
+} rk_term;
+int rk_combine(int32_t precision, int32_t coef_complex, int64_t m, const rk_term* terms, int32_t nterms, void* out,
+               void* stream);
+int rk_error_s(int32_t precision, int64_t m, const void* unew, const void* err, const rk_controller* ctl, int32_t q,
+               double* s_out, void* stream);
+
 /* Learned step-size controller (no counterpart in the reference).  Training kernels on a
  * batch of `batch` samples X[batch][RK_MLP_IN] with targets T[batch], FP32:
  *   rk_mlp_forward: Y[batch] = MLP(params; X)

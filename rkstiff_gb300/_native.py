@@ -60,6 +60,10 @@ class RkBatch(ctypes.Structure):
     ]
 
 
+class RkTerm(ctypes.Structure):
+    _fields_ = [("coef", ctypes.c_void_p), ("v", ctypes.c_void_p), ("w", ctypes.c_double)]
+
+
 class RkDenseBatch(ctypes.Structure):
     _fields_ = [
         ("method", ctypes.c_int32), ("n", ctypes.c_int32), ("n_inst", ctypes.c_int64),
@@ -93,7 +97,8 @@ assert STATE_DTYPE.itemsize == 128
 # every symbol the header declares
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
-           "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm")
+           "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
+           "rk_combine", "rk_error_s")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -149,6 +154,10 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_tf32x3_work_bytes.restype = i64
         lib.rk_tf32x3_gemm.argtypes = [vp, vp, vp, i64, i64, vp, vp]
         lib.rk_tf32x3_gemm.restype = ctypes.c_int
+        lib.rk_combine.argtypes = [i32, i32, i64, ctypes.POINTER(RkTerm), i32, vp, vp]
+        lib.rk_combine.restype = ctypes.c_int
+        lib.rk_error_s.argtypes = [i32, i64, vp, vp, ctypes.POINTER(RkController), i32, vp, vp]
+        lib.rk_error_s.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

@@ -282,6 +282,45 @@ class DiagEnsemble:
         self.launches += 1
         self.kernel_launches += int(np.count_nonzero(np.diff(self.class_start)))
 
+    def graph_launch(self, u_dev: torch.Tensor, u_src: torch.Tensor, t0, tf, h, max_steps: int = 200_000) -> None:
+        """One evolve launch from (u_src, t0, h) as a replay of a captured CUDA graph:
+        [u_dev <- u_src, state <- fresh state, rk_evolve (all class kernels)].  The graph is
+        captured on the first call for these buffers and parameters and replayed after."""
+        key = (u_dev.data_ptr(), u_src.data_ptr(), float(t0), float(tf), float(h), int(max_steps),
+               tuple(int(v) for v in (self.class_threads if self.class_threads is not None else ())),
+               tuple(int(v) for v in (self.class_groups if self.class_groups is not None else ())),
+               tuple(int(v) for v in (self.class_place if self.class_place is not None else ())),
+               None if self.mlp is None else self.mlp.data_ptr(), float(self.mlp_target),
+               None if self.attempt_log is None else self.attempt_log.data_ptr())
+        if getattr(self, "_graph_key", None) != key:
+            fresh = torch.from_numpy(np.ascontiguousarray(self.fresh_state(t0, tf, h)).view(np.uint8)).to(self.device)
+            # one ordinary launch first: creates the side streams and sets kernel attributes
+            u_dev.copy_(u_src)
+            self.state_dev.copy_(fresh)
+            self.launch(u_dev, nat.RK_RUN_EVOLVE, max_steps=max_steps)
+            torch.cuda.synchronize(self.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.device(self.device):
+                with torch.cuda.graph(g, capture_error_mode="relaxed"):
+                    u_dev.copy_(u_src)
+                    self.state_dev.copy_(fresh)
+                    self.launch(u_dev, nat.RK_RUN_EVOLVE, max_steps=max_steps)
+            self.launches -= 1  # the capture pass launched nothing
+            self.kernel_launches -= int(np.count_nonzero(np.diff(self.class_start)))
+            self._graph, self._graph_fresh, self._graph_key = g, fresh, key
+        if self.record_events:
+            stream = torch.cuda.current_stream(self.device)
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            self._graph.replay()
+            ev1.record(stream)
+            self.events.append((ev0, ev1))
+        else:
+            self._graph.replay()
+        self.launches += 1
+        self.kernel_launches += int(np.count_nonzero(np.diff(self.class_start)))
+
     def evolve(self, u_dev: torch.Tensor, t0, tf, h, store_freq: int = 0, snap_cap: int = 0,
                max_steps: int = 200_000, max_launches: int = 50, on_snapshots=None) -> np.ndarray:
         """Run every instance from (t0, h) to tf, relaunching while any instance paused

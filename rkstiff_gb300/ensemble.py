@@ -95,6 +95,36 @@ class Ensemble:
             raise
         return self.state
 
+    def evolve_graph(self, u_dev: torch.Tensor, u0_dev: torch.Tensor, t0: float, tf: float,
+                     h_init: Optional[float] = None, max_steps: int = 200_000, max_launches: int = 50) -> np.ndarray:
+        """evolve_packed from u0_dev into u_dev with the launch replayed from a captured CUDA
+        graph (the copy of the initial state, the state reset and every class kernel);
+        instances the launch bound paused are resumed with ordinary launches."""
+        if h_init is None:
+            if not self.adaptive:
+                raise ValueError("constant-step methods need h_init")
+            h_init = (tf - t0) / 100.0
+        h = tf - t0 if (self.adaptive and t0 + h_init > tf) else h_init
+        eng = self.engine
+        eng.graph_launch(u_dev, u0_dev, t0, tf, h, max_steps=max_steps)
+        st = eng.get_state()
+        paused = (nat.RK_ST_SNAP_FULL, nat.RK_ST_ITER_CAP)
+        for _ in range(max_launches - 1):
+            resume = np.isin(st["status"], paused)
+            if not np.any(resume):
+                break
+            st["snap_count"] = 0
+            st["status"] = np.where(resume, nat.RK_ST_RUNNING, st["status"])
+            eng.put_state(st)
+            eng.launch(u_dev, nat.RK_RUN_EVOLVE, max_steps=max_steps)
+            st = eng.get_state()
+        else:
+            if np.any(np.isin(st["status"], paused)):
+                self.state = st
+                raise EvolveBoundError(f"evolve did not reach tf within {max_launches} launches", st)
+        self.state = st
+        return st
+
     def evolve(self, u0s: Sequence, t0: float, tf: float, h_init: Optional[float] = None, **bounds):
         """Evolve all instances; returns the list of final spectra (device tensors).
         ``max_steps`` (accepted steps per launch) and ``max_launches`` bound the run."""

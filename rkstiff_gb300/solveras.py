@@ -127,10 +127,14 @@ class BaseSolverAS(BaseSolver):
     def _engine(self):
         if self._backend is None:
             from ._backend import DenseBackend, DiagBackend
-            if self._diag:
+            from ._callable import CallableBackend
+            from .models import BuiltinNL
+            if not self._diag:
+                self._backend = DenseBackend(self, self._method_name)
+            elif isinstance(self.nl_func, BuiltinNL):
                 self._backend = DiagBackend(self, self._method_name)
             else:
-                self._backend = DenseBackend(self, self._method_name)
+                self._backend = CallableBackend(self, self._method_name)
         return self._backend
 
     def reset(self) -> None:

@@ -25,9 +25,14 @@ class BaseSolverCS(BaseSolver):
     def _engine(self):
         if self._backend is None:
             from ._backend import DiagBackend
+            from ._callable import CallableBackend
+            from .models import BuiltinNL
             if not self._diag:
-                raise NotImplementedError(f"{type(self).__name__}: a 2-D operator needs the dense path")
-            self._backend = DiagBackend(self, self._method_name)
+                raise NotImplementedError(f"{type(self).__name__}: 2-D operators run ETD35 on the dense path")
+            if isinstance(self.nl_func, BuiltinNL):
+                self._backend = DiagBackend(self, self._method_name)
+            else:
+                self._backend = CallableBackend(self, self._method_name)
         return self._backend
 
     def reset(self) -> None:
