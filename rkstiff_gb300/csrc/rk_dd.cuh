@@ -1,0 +1,190 @@
+// Double-float ("dd") arithmetic: a value is an unevaluated sum hi + lo of two FP32 numbers
+// with |lo| <= ulp(hi)/2, about 48 significant bits, computed on the FP32 pipes (GB300 runs
+// FP64 at 1/64 of the FP32 rate).  Error-free transformations: Knuth's TwoSum, the FMA form
+// of Dekker's TwoProduct; the reciprocal by one Newton step from the FP32 reciprocal; exp by
+// range reduction x = k ln2 + r, r / 16 through a degree-7 Taylor polynomial of e^r - 1 and
+// four squarings of (1 + q) kept as q -> 2q + q^2 (so that e^x - 1 keeps its relative
+// accuracy for small x).
+//
+// Used for the ETD psi functions and coefficient combinations of real modes when the
+// coefficients are stored in FP32: their results match the FP64 evaluation after rounding
+// to FP32 (the combinations cancel by up to ~100x, which FP32 alone would not survive).
+#pragma once
+
+#include "rk_common.cuh"
+
+namespace rk {
+
+struct dd {
+  float hi, lo;
+};
+
+// compile-time split of a double constant
+struct ddc {
+  float hi, lo;
+  __host__ __device__ constexpr ddc(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+};
+
+RK_DEV dd two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return dd{s, (a - (s - bb)) + (b - bb)};
+}
+RK_DEV dd quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return dd{s, b - (s - a)};
+}
+RK_DEV dd two_prod(float a, float b) {
+  const float p = a * b;
+  return dd{p, fmaf(a, b, -p)};
+}
+
+RK_DEV dd dd_of(float a) { return dd{a, 0.f}; }
+RK_DEV dd dd_of(ddc c) { return dd{c.hi, c.lo}; }
+
+RK_DEV dd operator+(dd a, dd b) {
+  dd s = two_sum(a.hi, b.hi);
+  const dd t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+RK_DEV dd operator-(dd a) { return dd{-a.hi, -a.lo}; }
+RK_DEV dd operator-(dd a, dd b) { return a + (-b); }
+RK_DEV dd operator*(dd a, dd b) {
+  dd p = two_prod(a.hi, b.hi);
+  p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+  return quick_two_sum(p.hi, p.lo);
+}
+RK_DEV dd operator*(dd a, float b) {
+  dd p = two_prod(a.hi, b);
+  p.lo = fmaf(a.lo, b, p.lo);
+  return quick_two_sum(p.hi, p.lo);
+}
+RK_DEV dd operator*(float b, dd a) { return a * b; }
+RK_DEV dd operator*(dd a, ddc c) { return a * dd_of(c); }
+// exact scaling by a power of two
+RK_DEV dd scale2(dd a, float p2) { return dd{a.hi * p2, a.lo * p2}; }
+
+RK_DEV dd dd_recip(dd b) {
+  const float y0 = 1.0f / b.hi;
+  const dd e = dd_of(1.f) - b * y0;  // 1 - b y0, small
+  return dd_of(y0) + e * y0;
+}
+
+// e^x for x.hi in [-87, 80] and em1 = e^x - 1, each to ~2^-46 relative: x = k ln2 + r,
+// q = e^(r/16) - 1 by its Taylor polynomial, four squarings q -> 2q + q^2 give e^r - 1; em1
+// is q itself when k = 0 (no cancellation for small x) and e - 1 otherwise (|e^x - 1| >
+// 0.29 there).  Below -87, e = 0 and em1 = -1 (e^x is below FP32 range).
+RK_DEV dd dd_exp(dd xin, dd& em1) {
+  // branch-free, so that independent evaluations interleave: clamp, then select
+  const bool under = xin.hi < -87.f;
+  const dd x = under ? dd{-87.f, 0.f} : xin;
+  constexpr ddc LN2(0.6931471805599453);
+  const float k = rintf(x.hi * 1.44269504f);
+  dd r = x - dd_of(LN2) * k;
+  r = scale2(r, 0.0625f);  // |r| <= ln2/32
+  // q = e^r - 1 = r (1 + r/2 (1 + r/3 (... (1 + r/7))))
+  constexpr ddc I3(1.0 / 3.0), I5(1.0 / 5.0), I6(1.0 / 6.0), I7(1.0 / 7.0);
+  dd q = dd_of(1.f) + r * dd_of(I7);
+  q = dd_of(1.f) + (r * dd_of(I6)) * q;
+  q = dd_of(1.f) + (r * dd_of(I5)) * q;
+  q = dd_of(1.f) + scale2(r, 0.25f) * q;
+  q = dd_of(1.f) + (r * dd_of(I3)) * q;
+  q = dd_of(1.f) + scale2(r, 0.5f) * q;
+  q = r * q;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q = scale2(q, 2.f) + q * q;
+  const dd e1 = dd_of(1.f) + q;
+  const int ki = (int)k;
+  const dd e{ldexpf(e1.hi, ki), ldexpf(e1.lo, ki)};
+  em1 = under ? dd_of(-1.f) : (ki == 0 ? q : e - dd_of(1.f));
+  return under ? dd{0.f, 0.f} : e;
+}
+
+RK_DEV dd dd_from_double(double v) {
+  const float hi = (float)v;
+  return dd{hi, (float)(v - (double)hi)};
+}
+
+// FP32 ETD coefficients of a real mode z = h lambda (|z| >= modecutoff, z <= 80) in
+// double-float arithmetic, h given as a double-float: method ETD35/ETD5 (21 values, layout
+// C35_*) or ETD34/ETD4 (10, C34_*).  The psi forms are those of fast_real_psi, reassociated
+// so that no intermediate leaves FP32 range for |z| up to ~1e18; the combinations follow
+// etd_from_psi_e.
+RK_DEV void dd_etd_coeffs(int method, double zd, dd h, float* o) {
+  const dd z = dd_from_double(zd);
+  const dd rz = dd_recip(z);
+  // h psi_1..3 of x = c z from e^x - 1 and r = 1/x
+  auto psis = [&](dd x, dd em1, dd r, dd* P, bool third) {
+    const dd d = em1 - x;
+    const dd dr = d * r;
+    P[0] = h * (em1 * r);
+    P[1] = scale2(h, 2.f) * (dr * r);
+    if (third) P[2] = (h * 6.f) * (r * (dr * r - dd_of(0.5f)));
+  };
+  // one exponential: e^(z/4) and m1 = e^(z/4) - 1; the other scales by products, e^(cz)
+  // from e1 (relative accuracy for stiff modes) and e^(cz) - 1 from m1 through
+  // (1 + m)^2 - 1 = m (m + 2) (relative accuracy for small z)
+  dd m1;
+  const dd e1 = dd_exp(scale2(z, 0.25f), m1);
+  const dd e2 = e1 * e1;
+  const dd m2 = m1 * (m1 + dd_of(2.f));
+  const dd e4 = e2 * e2;
+  const dd m4 = m2 * (m2 + dd_of(2.f));
+  if (method == RK_ETD35 || method == RK_ETD5) {
+    constexpr ddc F43(4.0 / 3.0);
+    const dd z34 = z * 0.75f;
+    const dd e3 = e2 * e1;
+    const dd m3 = (m1 + m2) + m1 * m2;
+    dd P[9];
+    psis(scale2(z, 0.25f), m1, scale2(rz, 4.f), P + 0, false);
+    psis(scale2(z, 0.5f), m2, scale2(rz, 2.f), P + 2, false);
+    psis(z34, m3, rz * dd_of(F43), P + 4, false);
+    psis(z, m4, rz, P + 6, true);
+    const dd p1_14 = P[0], p2_14 = P[1], p1_12 = P[2], p2_12 = P[3], p1_34 = P[4], p2_34 = P[5];
+    const dd p1 = P[6], p2 = P[7], p3 = P[8];
+    constexpr ddc R42(1.0 / 42), R7(1.0 / 7), R28(1.0 / 28), R84(1.0 / 84), R2700(1.0 / 2700), R1350(1.0 / 1350),
+        R225(1.0 / 225);
+    o[C35_E14] = e1.hi;
+    o[C35_E12] = e2.hi;
+    o[C35_E34] = e3.hi;
+    o[C35_E] = e4.hi;
+    o[C35_A21] = scale2(p1_14, 0.25f).hi;
+    o[C35_A31] = scale2(p1_14 - scale2(p2_14, 0.5f), 0.25f).hi;
+    o[C35_A32] = scale2(p2_14, 0.125f).hi;
+    o[C35_A41] = scale2(p1_12 - p2_12, 0.5f).hi;
+    o[C35_A43] = scale2(p2_12, 0.5f).hi;
+    o[C35_A51] = scale2((p1_34 - scale2(p2_34 * 3.f, 0.25f)) * 3.f, 0.25f).hi;
+    o[C35_A52] = scale2(p1_34 * -3.f, 0.125f).hi;
+    o[C35_A54] = scale2(p2_34 * 9.f, 0.0625f).hi;
+    o[C35_A61] = ((p1 * -77.f + p2 * 59.f) * R42).hi;
+    o[C35_A62] = ((p1 * 8.f) * R7).hi;
+    o[C35_A63] = ((p1 * 111.f - p2 * 87.f) * R28).hi;
+    o[C35_A65] = ((p1 * -47.f + p2 * 143.f) * R84).hi;
+    o[C35_A71] = (((p1 * 257.f - p2 * 497.f) + p3 * 270.f) * 7.f * R2700).hi;
+    o[C35_A73] = (((p1 * 1097.f - p2 * 467.f) - p3 * 150.f) * R1350).hi;
+    o[C35_A74] = (scale2((p1 * -49.f + p2 * 199.f) - p3 * 135.f, 2.f) * R225).hi;
+    o[C35_A75] = (((p1 * -313.f + p2 * 883.f) - p3 * 90.f) * R1350).hi;
+    o[C35_A76] = (((p1 * 509.f - p2 * 2129.f) + p3 * 1830.f) * R2700).hi;
+  } else {
+    dd P[5];
+    psis(scale2(z, 0.5f), m2, scale2(rz, 2.f), P + 0, false);
+    psis(z, m4, rz, P + 2, true);
+    const dd p1_12 = P[0], p2_12 = P[1], p1 = P[2], p2 = P[3], p3 = P[4];
+    constexpr ddc T23(2.0 / 3.0);
+    o[C34_E] = e4.hi;
+    o[C34_E2] = e2.hi;
+    o[C34_A21] = scale2(p1_12, 0.5f).hi;
+    o[C34_A31] = scale2(p1_12 - p2_12, 0.5f).hi;
+    o[C34_A32] = scale2(p2_12, 0.5f).hi;
+    o[C34_A41] = (p1 - p2).hi;
+    o[C34_A43] = p2.hi;
+    o[C34_A51] = ((p1 - p2 * 1.5f) + p3 * T23).hi;
+    o[C34_A52] = (p2 - p3 * T23).hi;
+    o[C34_A54] = (scale2(p2, -0.5f) + p3 * T23).hi;
+  }
+}
+
+}  // namespace rk

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "rk_coeffs.cuh"
+#include "rk_dd.cuh"
 #include "rk_common.cuh"
 #include "rk_fft.cuh"
 #include "rk_mlp.cuh"
@@ -269,6 +270,7 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
+  const dd hdd = dd_from_double(h);
   // pass 1: thread per mode, direct formula for |z| >= modecutoff; with FAST the small
   // modes are evaluated here too, by the Taylor series of psi_k (see taylor_psi)
   for (int j = g.tid; j < m; j += g.nthr) {
@@ -287,7 +289,20 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
         continue;
       }
     }
-    if constexpr (FAST && sizeof(S) == sizeof(double)) {
+    if constexpr (FAST && sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float)) {
+      const double zr = sre(z);
+      if (zr <= 80.0) {
+        // double-float on the FP32 pipes; the result rounds to the FP64 evaluation's
+        float of[NC];
+        dd_etd_coeffs(METHOD, zr, hdd, of);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+        continue;
+      }
+      double E[4];
+      fast_real_psi(METHOD, zr, h, E, reinterpret_cast<double*>(P));
+      etd_from_psi_e<double>(METHOD, E, reinterpret_cast<double*>(P), reinterpret_cast<double*>(o));
+    } else if constexpr (FAST && sizeof(S) == sizeof(double)) {
       double E[4];
       fast_real_psi(METHOD, sre(z), h, E, reinterpret_cast<double*>(P));
       etd_from_psi_e<double>(METHOD, E, reinterpret_cast<double*>(P), reinterpret_cast<double*>(o));

@@ -283,3 +283,31 @@ def test_fp32_nls(golden):
     s = rk.ETD35(lin, nl, config=rk.SolverConfig(epsilon=1e-6), device_options=rk.DeviceOptions(precision="fp32"))
     u = s.evolve(g["nls256_u0"], 0.0, 2.0, store_data=False)
     assert rel(u, g["nls256_ETD35_final"]) < 1e-4
+
+
+@pytest.mark.parametrize("method", ["ETD35", "ETD5", "ETD34", "ETD4"])
+@pytest.mark.parametrize("h", [1e-3, 0.1, 1.7])
+def test_fp32_coefficients_round_fp64(method, h):
+    """FP32 coefficients of a real operator (evaluated in double-float on the FP32 pipes)
+    against the FP64 evaluation rounded to FP32 over z = h lambda from -1e9 to +50 (stiff,
+    moderate, near the modecutoff, growing modes): within 4 FP32 ulps plus 1e-13 |z|
+    relative for |z| >= modecutoff (the double-float path).  The second term covers the stiffest modes, where combinations such as ETD34
+    a51 = psi1 - 1.5 psi2 + 2/3 psi3 cancel their O(h/z) parts down to O(h/z^2), by ~|z|;
+    the 48-bit double-float leaves ~1e-14 |z| relative there (FP64 itself 1e-16 |z|), on
+    coefficients of size ~h/z^2 whose contribution is below FP32 resolution."""
+    lam = np.concatenate([-np.logspace(-6, 9, 300), np.logspace(-6, np.log10(50.0 / h), 60), [0.0]])
+    order = ETD35_ORDER if method in ("ETD35", "ETD5") else ETD34_ORDER
+    c32 = device_coeffs(method, lam, h, nat.RK_FP32).real
+    c64 = device_coeffs(method, lam, h, nat.RK_FP64).real
+    r32 = c64.astype(np.float32).astype(np.float64)
+    ulp = np.spacing(np.abs(r32).astype(np.float32)).astype(np.float64)
+    zmag = np.maximum(1.0, np.abs(h * lam))
+    # below the modecutoff both precisions use small-mode series (FP32 storage: Taylor;
+    # FP64: the reference's contour mean), whose ~1/z cancellation in combinations such as
+    # a41 = (psi1 - psi2)/2 leaves them ~1e-16/|z| apart: compared on the array's scale
+    direct = np.abs(h * lam) >= 0.01
+    for i, name in enumerate(order):
+        bad = direct & (np.abs(c32[i] - r32[i]) > 4 * ulp[i] + 1e-13 * zmag * np.abs(r32[i]) + 1e-37)
+        assert not np.any(bad), (method, h, name, lam[bad][:3], c32[i][bad][:3], r32[i][bad][:3])
+        small = ~direct
+        assert np.max(np.abs(c32[i][small] - c64[i][small])) <= 1e-6 * np.max(np.abs(c64[i])), (method, h, name)
