@@ -1,23 +1,22 @@
 // Dense (non-diagonal) operator path: ETD35 for a batch of instances that share one n x n
 // lin_op (n <= 128), on the fifth-generation tensor cores.
 //
-// Replaces rkstiff/etd35.py:_Etd35NonDiagonal (etd35.py:498-720).  Per attempt, four
+// Replaces rkstiff/etd35.py:_Etd35NonDiagonal (etd35.py:498-720).  Per attempt, two
 // kernels, each a no-op once the batch has left RK_ST_RUNNING (so a fixed launch sequence
 // can run ahead of the host):
-//   coef_diag_kernel    when h changed: the 21 diagonal ETD35 coefficient functions of
-//                       h * eig in FP64 (the reference's diagonalized arithmetic,
-//                       etd35.py:348-495, with its contour mean for small |z|)
-//   coef_matrix_kernel  when h changed: M_c = S diag(c) S^-1 in FP64 for every coefficient
-//                       (the psi-matrices of etd35.py:602-658), stored as a TF32 hi/lo pair
-//   attempt_kernel      one CTA per 64 instances: the ETD35 stages (etd35.py:690-720) as
-//                       six K-concatenated GEMM chains, e.g. k3 = [E14 a31 a32] [u; N1; N2],
-//                       run as 3xTF32 tcgen05.mma (A_lo B_hi + A_hi B_lo + A_hi B_hi, FP32
-//                       accumulate in tensor memory) fed by TMA through a 4-slot mbarrier
-//                       ring; the Allen-Cahn nonlinearity, the stage combinations, the new
-//                       state and the per-instance error test (solveras.py:412-455) run in
-//                       the epilogues
-//   control_kernel      the smallest s of the batch goes through the reference's
-//                       accept/reject rule (solveras.py:457-554); the batch steps in lockstep
+//   coef_kernel     when h changed: every block evaluates the 21 diagonal ETD35 coefficient
+//                   functions of h * eig in FP64 (the reference's diagonalized arithmetic,
+//                   etd35.py:348-495, with its contour mean for small |z|) and forms one tile
+//                   of one matrix M_c = S diag(c) S^-1 in FP64 (the psi-matrices of
+//                   etd35.py:602-658), stored as a TF32 hi/lo pair
+//   attempt_kernel  one CTA per 64 instances: the ETD35 stages (etd35.py:690-720) as six
+//                   K-concatenated GEMM chains, e.g. k3 = [E14 a31 a32] [u; N1; N2], run as
+//                   3xTF32 tcgen05.mma (A_lo B_hi + A_hi B_lo + A_hi B_hi, FP32 accumulate in
+//                   tensor memory) fed by TMA through a 4-slot mbarrier ring; the Allen-Cahn
+//                   nonlinearity, the stage combinations, the new state and the per-instance
+//                   error test (solveras.py:412-455) run in the epilogues; the last CTA to
+//                   finish puts the batch's smallest s through the reference's accept/reject
+//                   rule (solveras.py:457-554): the batch steps in lockstep
 //
 // Vectors live in global memory instance-major (each instance's 128 values contiguous, K
 // innermost for the B operand) as FP32 hi/lo pairs; the working set (11 vectors x 8192
@@ -52,7 +51,7 @@ constexpr int ATTEMPT_SMEM = 1024 + NS * SLOT_BYTES + 256;
 enum { V_U0, V_U1, V_N1, V_N2, V_N3, V_N4, V_N5, V_N6, V_D23, V_D24, V_EV, NVEC };
 
 struct Layout {  // byte offsets into the work buffer
-  int64_t bpad, a, v, cd, eig, S, Si, shift, s, total;
+  int64_t bpad, a, v, cd, eig, S, Si, shift, s, cmin, ctr, total;
 };
 RK_HD int64_t al1k(int64_t x) { return (x + 1023) & ~int64_t(1023); }
 inline Layout layout(int64_t n_inst) {
@@ -75,6 +74,10 @@ inline Layout layout(int64_t n_inst) {
   o = al1k(o + (int64_t)DM * 4);
   L.s = o;
   o = al1k(o + L.bpad * 8);
+  L.cmin = o;
+  o = al1k(o + (L.bpad / NT) * 8);
+  L.ctr = o;
+  o = al1k(o + 64);
   L.total = o;
   return L;
 }
@@ -89,6 +92,8 @@ struct Params {
   const double* Si;      // [DM][DM]
   const float* shift;    // [DM]
   double* s;             // [bpad]
+  double* cmin;          // [bpad / NT] smallest s of each CTA's instances (NaN: any NaN)
+  unsigned int* ctr;     // CTAs of the current attempt that have finished
   int64_t n_inst, bpad;
   int n;
   rk_controller ctl;
@@ -128,6 +133,7 @@ __global__ void pad_kernel(Params p, const double* eig, const double* S, const d
     const_cast<float*>(p.shift)[i] = i < p.n ? (float)shift[i] : 0.f;
   }
   if (i < (int64_t)NCOEF * DM) p.Cd[i] = 0.0;
+  if (i == 0) *p.ctr = 0u;
 }
 
 // caller's states (n_inst x n) into the current state vector, zero-padded
@@ -151,40 +157,32 @@ __global__ void store_u_kernel(Params p, float* u) {
 // ---------------------------------------------------------------------------------
 // coefficients (FP64)
 // ---------------------------------------------------------------------------------
-__global__ void coef_diag_kernel(Params p) {
-  rk_dense_state* st = p.st;
+// When h differs from the h of the current matrices (exact compare, as etd35.py:851): every
+// block evaluates the 21 diagonal coefficient functions of h * eig in FP64 into shared
+// memory, then forms one 32 x 32 tile of one matrix M_c = S diag(c) S^-1.  h_coeff is
+// advanced by the attempt that uses the matrices.
+__global__ void __launch_bounds__(256) coef_kernel(Params p) {
+  const rk_dense_state* st = p.st;
   if (st->status != RK_ST_RUNNING) return;
   const double h = st->h;
-  const bool same = h == st->h_coeff;  // exact compare, as etd35.py:851
-  __syncthreads();
-  if (same) {
-    if (threadIdx.x == 0) st->need_matrix = 0;
-    return;
-  }
-  Group g{(int)threadIdx.x, (int)blockDim.x, 0};
-  compute_coeffs_impl<double, double, RK_ETD35, false>(g, p.n, DM, p.eig, p.Cd, h, p.ec);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    st->h_coeff = h;
-    st->need_matrix = 1;
-    st->coeff_updates += 1;
-  }
-}
-
-// M_c[i][j] = sum_k S[i][k] c_k Sinv[k][j]: one 32 x 32 tile of one matrix per block
-__global__ void __launch_bounds__(256) coef_matrix_kernel(Params p) {
-  const rk_dense_state* st = p.st;
-  if (st->status != RK_ST_RUNNING || st->need_matrix == 0) return;
+  if (h == st->h_coeff) return;
+  __shared__ double Cd[NCOEF * DM];
   __shared__ double Ss[32][33];
   __shared__ double Sis[32][33];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < NCOEF * DM; e += 256) Cd[e] = 0.0;
+  __syncthreads();
+  Group g{tid, 256, 0};
+  compute_coeffs_impl<double, double, RK_ETD35, false>(g, p.n, DM, p.eig, Cd, h, p.ec);
+  __syncthreads();
   const int c = blockIdx.y;
   const int i0 = (blockIdx.x >> 2) * 32, j0 = (blockIdx.x & 3) * 32;
-  const int tid = threadIdx.x, r = tid >> 3, q0 = (tid & 7) * 4;
+  const int r = tid >> 3, q0 = (tid & 7) * 4;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k0 = 0; k0 < DM; k0 += 32) {
     for (int e = tid; e < 32 * 32; e += 256) {
       const int a = e >> 5, b = e & 31;
-      Ss[a][b] = p.S[(i0 + a) * DM + k0 + b] * p.Cd[c * DM + k0 + b];
+      Ss[a][b] = p.S[(i0 + a) * DM + k0 + b] * Cd[c * DM + k0 + b];
       Sis[a][b] = p.Si[(k0 + a) * DM + j0 + b];
     }
     __syncthreads();
@@ -222,13 +220,15 @@ struct Ring {
   uint64_t* empty;
 };
 
-// Issued by one thread.  `g` numbers chunks over the whole kernel (mbarrier parities).
-// Returns false when a wait timed out.
+// The two roles of a chain, each run by one thread at the same time: the producer keeps the
+// ring full (a slot is refilled once the MMAs that read it have completed), the MMA thread
+// issues each chunk as soon as its tiles have landed.  `g` numbers chunks over the whole
+// kernel (mbarrier parities); both roles advance it identically.  Return false when a wait
+// timed out.
 template <class ChunkFn>
-RK_DEV bool run_chain(int nch, ChunkFn chunk, int& g, const Ring& ring, uint32_t tmem, const CUtensorMap* tmA,
-                      const CUtensorMap* tmB) {
-  constexpr uint32_t idesc = tc::idesc_tf32(DM, NT);
-  auto issue = [&](int i) -> bool {
+RK_DEV bool chain_producer(int nch, ChunkFn chunk, int& g, const Ring& ring, const CUtensorMap* tmA,
+                           const CUtensorMap* tmB) {
+  for (int i = 0; i < nch; ++i) {
     const int gi = g + i, slot = gi % NS;
     if (gi >= NS && !tc::mbar_wait(&ring.empty[slot], (uint32_t)((gi / NS) - 1) & 1u, WAIT_NS)) return false;
     const ChunkCoord cc = chunk(i);
@@ -238,10 +238,14 @@ RK_DEV bool run_chain(int nch, ChunkFn chunk, int& g, const Ring& ring, uint32_t
     tc::tma_load_2d(base + A_TILE, tmA, &ring.full[slot], cc.k0, cc.a_lo);
     tc::tma_load_2d(base + 2 * A_TILE, tmB, &ring.full[slot], cc.k0, cc.b_hi);
     tc::tma_load_2d(base + 2 * A_TILE + B_TILE, tmB, &ring.full[slot], cc.k0, cc.b_lo);
-    return true;
-  };
-  for (int i = 0; i < nch && i < NS; ++i)
-    if (!issue(i)) return false;
+  }
+  g += nch;
+  return true;
+}
+
+template <class ChunkFn>
+RK_DEV bool chain_mma(int nch, ChunkFn chunk, int& g, const Ring& ring, uint32_t tmem) {
+  constexpr uint32_t idesc = tc::idesc_tf32(DM, NT);
   for (int i = 0; i < nch; ++i) {
     const int gi = g + i, slot = gi % NS;
     if (!tc::mbar_wait(&ring.full[slot], (uint32_t)(gi / NS) & 1u, WAIT_NS)) return false;
@@ -260,7 +264,6 @@ RK_DEV bool run_chain(int nch, ChunkFn chunk, int& g, const Ring& ring, uint32_t
       tc::mma_tf32(d, ahi + o, bhi + o, idesc, 1u);
     }
     tc::mma_commit(&ring.empty[slot]);
-    if (i + NS < nch && !issue(i + NS)) return false;
   }
   g += nch;
   return true;
@@ -275,9 +278,61 @@ RK_DEV void load_acc(uint32_t tmem, int warp, int acc, float* v) {
   tc::tmem_ld_wait();
 }
 
+// 32 columns [half*32, half*32+32) of accumulator acc
+RK_DEV void load_acc_half(uint32_t tmem, int warp, int acc, int half, float* v) {
+  __syncwarp();
+  const uint32_t base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(acc * NT + half * 32);
+  tc::tmem_ld16(base, v);
+  tc::tmem_ld16(base + 16u, v + 16);
+  tc::tmem_ld_wait();
+}
+
 struct Term {
   int coef, vec, acc;
 };
+
+// The reference's accept/reject rule (solveras.py:457-554) on the batch's smallest s; one
+// thread, after every CTA of the attempt has written its instances' s.  h_coeff records
+// the h the attempt's matrices were built for.
+RK_DEV void apply_controller(const Params& p, double s) {
+  rk_dense_state* st = p.st;
+  const rk_controller& ctl = p.ctl;
+  if (st->error) {
+    st->status = RK_E_CUDA;  // a device wait timed out: stop (the host reports it)
+    return;
+  }
+  const double h = st->h;
+  if (h != st->h_coeff) {
+    st->h_coeff = h;
+    st->coeff_updates += 1;
+  }
+  st->attempts += 1;
+  st->nl_evals += 5 + st->n1_fresh;
+  st->s_last = s;
+  if (isinf(s) || isnan(s) || s < 1.0) {
+    st->accept = 0;
+    st->n1_fresh = 0;
+    st->rejects += 1;
+    st->h = reject_h(s, h, ctl);
+    st->numloops += 1;
+    if (st->numloops > 50) st->status = RK_ST_MAX_LOOPS;
+    else if (st->h < ctl.minh) st->status = RK_ST_MIN_STEP;
+  } else {
+    st->accept = 1;
+    st->n1_fresh = 1;
+    st->cur ^= 1;
+    const double t = st->t + h;
+    st->t = t;
+    st->steps += 1;
+    st->numloops = 0;
+    const double hs = accept_h(s, h, ctl);
+    st->h_suggest = hs;
+    const double hn = (t + hs > st->tf) ? st->tf - t : hs;
+    st->h = hn;
+    if (!(t < st->tf)) st->status = RK_ST_DONE;
+    else if (t + hn == t) st->status = RK_ST_MIN_STEP;
+  }
+}
 
 // ---------------------------------------------------------------------------------
 // one ETD35 attempt for NT instances
@@ -315,9 +370,17 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     tc::tmem_alloc(tmem_slot, 2 * NT);
     tc::tmem_relinquish();
   }
-  // N1 = N(u) (pointwise; thread = row)
+  // N1 = N(u) (pointwise; thread = row).  ev accumulates the error combination
+  // -N1 + 4 N3 - 6 N4 + 4 N5 - N6 (etd35.py:344) in registers as the stages arrive, and
+  // n2 keeps N2 for N2 - N3 and N2 - 3 N4 / 2, so no epilogue reads a stage vector back.
   const float xr = p.shift[row];
-  for (int j = 0; j < NT; ++j) vput(p, V_N1, col0 + j, row, nl_ac(vget(p, vU, col0 + j, row), xr));
+  float ev[NT], n2[NT];
+#pragma unroll 16
+  for (int j = 0; j < NT; ++j) {
+    const float n1 = nl_ac(vget(p, vU, col0 + j, row), xr);
+    vput(p, V_N1, col0 + j, row, n1);
+    ev[j] = -n1;
+  }
   tc::fence_proxy_async_global();
   tc::tc_fence_before();
   __syncthreads();
@@ -337,30 +400,36 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   const int nterms[6] = {2, 3, 3, 4, 5, 7};
 
   int g = 0;
-  float acc[NT];
+  float acc[32];
   for (int ch = 0; ch < 6; ++ch) {
-    if (tid == 0) {
-      if (!*abort_flag) {
-        const Term* terms = chains[ch];
-        const int64_t bpad = p.bpad;
-        auto chunk = [&](int i) {
-          const Term& t = terms[i >> 2];
-          ChunkCoord cc;
-          cc.k0 = (i & 3) * KC;
-          cc.a_hi = (t.coef * 2) * DM;
-          cc.a_lo = (t.coef * 2 + 1) * DM;
-          cc.b_hi = (int)((t.vec * 2) * bpad + col0);
-          cc.b_lo = (int)((t.vec * 2 + 1) * bpad + col0);
-          cc.acc = t.acc;
-          cc.first = (i & 3) == 0 && ((i >> 2) == 0 || terms[(i >> 2) - 1].acc != t.acc);
-          return cc;
-        };
-        if (!run_chain(nterms[ch] * (DM / KC), chunk, g, ring, tmem, &tmA, &tmV)) {
+    if (tid == 0 || tid == 32) {
+      const Term* terms = chains[ch];
+      const int64_t bpad = p.bpad;
+      auto chunk = [&](int i) {
+        const Term& t = terms[i >> 2];
+        ChunkCoord cc;
+        cc.k0 = (i & 3) * KC;
+        cc.a_hi = (t.coef * 2) * DM;
+        cc.a_lo = (t.coef * 2 + 1) * DM;
+        cc.b_hi = (int)((t.vec * 2) * bpad + col0);
+        cc.b_lo = (int)((t.vec * 2 + 1) * bpad + col0);
+        cc.acc = t.acc;
+        cc.first = (i & 3) == 0 && ((i >> 2) == 0 || terms[(i >> 2) - 1].acc != t.acc);
+        return cc;
+      };
+      const int nch = nterms[ch] * (DM / KC);
+      if (tid == 32) {
+        if (!*abort_flag && !chain_producer(nch, chunk, g, ring, &tmA, &tmV)) {
           atomicOr(&st->error, 1);
           *abort_flag = 1;
         }
+      } else {
+        if (!*abort_flag && !chain_mma(nch, chunk, g, ring, tmem)) {
+          atomicOr(&st->error, 1);
+          *abort_flag = 1;
+        }
+        tc::mma_commit(accb);  // arrives once every MMA issued so far has completed
       }
-      tc::mma_commit(accb);  // arrives once every MMA issued so far has completed
     }
     if (!tc::mbar_wait(accb, (uint32_t)ch & 1u, WAIT_NS)) {
       atomicOr(&st->error, 2);
@@ -369,28 +438,32 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     tc::tc_fence_after();
     __syncthreads();
     if (*abort_flag) break;
-    load_acc(tmem, warp, 0, acc);
     if (ch < 5) {
-#pragma unroll 4
-      for (int j = 0; j < NT; ++j) {
-        const int64_t c = col0 + j;
-        const float nk = nl_ac(acc[j], xr);
-        switch (ch) {
-          case 0: vput(p, V_N2, c, row, nk); break;
-          case 1:
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        load_acc_half(tmem, warp, 0, half, acc);
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int j = half * 32 + jj;
+          const int64_t c = col0 + j;
+          const float nk = nl_ac(acc[jj], xr);
+          if (ch == 0) {
+            vput(p, V_N2, c, row, nk);
+            n2[j] = nk;
+          } else if (ch == 1) {
             vput(p, V_N3, c, row, nk);
-            vput(p, V_D23, c, row, vget(p, V_N2, c, row) - nk);
-            break;
-          case 2:
+            vput(p, V_D23, c, row, n2[j] - nk);
+            ev[j] = ev[j] + 4.f * nk;
+          } else if (ch == 2) {
             vput(p, V_N4, c, row, nk);
-            vput(p, V_D24, c, row, vget(p, V_N2, c, row) - (3.f * nk) * 0.5f);
-            break;
-          case 3: vput(p, V_N5, c, row, nk); break;
-          default: {
+            vput(p, V_D24, c, row, n2[j] - (3.f * nk) * 0.5f);
+            ev[j] = ev[j] - 6.f * nk;
+          } else if (ch == 3) {
+            vput(p, V_N5, c, row, nk);
+            ev[j] = ev[j] + 4.f * nk;
+          } else {
             vput(p, V_N6, c, row, nk);
-            const float ev = (((-vget(p, V_N1, c, row) + 4.f * vget(p, V_N3, c, row)) - 6.f * vget(p, V_N4, c, row)) +
-                              4.f * vget(p, V_N5, c, row)) - nk;
-            vput(p, V_EV, c, row, ev);
+            vput(p, V_EV, c, row, ev[j] - nk);
           }
         }
       }
@@ -401,15 +474,21 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     } else {
       // new state and the per-instance error test on it (solveras.py:412-455); the ring's
       // shared memory is free: every MMA that read it has completed
-      float err[NT];
-      load_acc(tmem, warp, 1, err);
       constexpr int LD = NT + 1;
       float* ru = reinterpret_cast<float*>(sm);
       float* re = ru + DM * LD;
-      for (int j = 0; j < NT; ++j) {
-        vput(p, vUN, col0 + j, row, acc[j]);
-        ru[row * LD + j] = acc[j] * acc[j];
-        re[row * LD + j] = err[j] * err[j];
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        float err[32];
+        load_acc_half(tmem, warp, 0, half, acc);
+        load_acc_half(tmem, warp, 1, half, err);
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int j = half * 32 + jj;
+          vput(p, vUN, col0 + j, row, acc[jj]);
+          ru[row * LD + j] = acc[jj] * acc[jj];
+          re[row * LD + j] = err[jj] * err[jj];
+        }
       }
       __syncthreads();
       const int j = tid >> 1, half = tid & 1;
@@ -435,17 +514,37 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
       }
       au = df_add(au, df{__shfl_xor_sync(0xffffffffu, au.hi, 1), __shfl_xor_sync(0xffffffffu, au.lo, 1)});
       ae = df_add(ae, df{__shfl_xor_sync(0xffffffffu, ae.hi, 1), __shfl_xor_sync(0xffffffffu, ae.lo, 1)});
-      if (half == 0 && col0 + j < p.n_inst) {
+      double s = INFINITY;  // padding columns do not take part
+      if (col0 + j < p.n_inst) {
         const double su = (double)au.hi + (double)au.lo, se = (double)ae.hi + (double)ae.lo;
         const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
-        double s;
         if (ratio != ratio || isinf(ratio)) {
           s = p.ctl.safety_f * ratio;
         } else {
           const float rf = (float)fmin(ratio, 1e30);
           s = p.ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / 4.f));  // q = 4
         }
-        p.s[col0 + j] = s;
+        if (half == 0) p.s[col0 + j] = s;
+      }
+      // the CTA's smallest s (NaN if any is NaN) for the batch controller
+      int snan = s != s;
+      double smin = snan ? INFINITY : s;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) smin = fmin(smin, __shfl_xor_sync(0xffffffffu, smin, o));
+      snan = __any_sync(0xffffffffu, snan);
+      __shared__ double cm[4];
+      __shared__ int cn[4];
+      if ((tid & 31) == 0) {
+        cm[warp] = smin;
+        cn[warp] = snan;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        for (int i = 1; i < 4; ++i) {
+          smin = fmin(smin, cm[i]);
+          snan |= cn[i];
+        }
+        p.cmin[blockIdx.x] = snan ? nan_d() : smin;
       }
     }
   }
@@ -457,72 +556,42 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem, 2 * NT);
   }
-}
-
-// ---------------------------------------------------------------------------------
-// lockstep controller: min s over the batch through the reference's rules
-// ---------------------------------------------------------------------------------
-__global__ void control_kernel(Params p) {
-  rk_dense_state* st = p.st;
-  if (st->status != RK_ST_RUNNING) return;
-  __shared__ double wmin[32];
-  __shared__ int wnan[32];
+  // The last CTA to finish applies the lockstep controller to the batch's smallest s.
+  // Every CTA read the state before incrementing the counter, so the update cannot race
+  // with a reader of this attempt.
+  __shared__ int last;
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(p.ctr, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double wmin[4];
+  __shared__ int wnan[4];
   double m = INFINITY;
   int nan = 0;
-  for (int64_t i = threadIdx.x; i < p.n_inst; i += blockDim.x) {
-    const double s = p.s[i];
+  for (int i = tid; i < (int)gridDim.x; i += ATTEMPT_THREADS) {
+    const double s = __ldcg(p.cmin + i);
     if (s != s) nan = 1;
     else m = fmin(m, s);
   }
-  m = fmin(m, __shfl_xor_sync(0xffffffffu, m, 16));
-  m = fmin(m, __shfl_xor_sync(0xffffffffu, m, 8));
-  m = fmin(m, __shfl_xor_sync(0xffffffffu, m, 4));
-  m = fmin(m, __shfl_xor_sync(0xffffffffu, m, 2));
-  m = fmin(m, __shfl_xor_sync(0xffffffffu, m, 1));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
   nan = __any_sync(0xffffffffu, nan);
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    wmin[w] = m;
-    wnan[w] = nan;
+  if ((tid & 31) == 0) {
+    wmin[warp] = m;
+    wnan[warp] = nan;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  for (int i = 0; i < nw; ++i) {
-    m = fmin(m, wmin[i]);
-    nan |= wnan[i];
-  }
-  const double s = nan ? nan_d() : m;
-  const rk_controller& ctl = p.ctl;
-  if (st->error) {
-    st->status = RK_E_CUDA;  // a device wait timed out: stop (the host reports it)
-    return;
-  }
-  st->attempts += 1;
-  st->nl_evals += 5 + st->n1_fresh;
-  st->s_last = s;
-  const double h = st->h;
-  if (isinf(s) || isnan(s) || s < 1.0) {
-    st->accept = 0;
-    st->n1_fresh = 0;
-    st->rejects += 1;
-    st->h = reject_h(s, h, ctl);
-    st->numloops += 1;
-    if (st->numloops > 50) st->status = RK_ST_MAX_LOOPS;
-    else if (st->h < ctl.minh) st->status = RK_ST_MIN_STEP;
-  } else {
-    st->accept = 1;
-    st->n1_fresh = 1;
-    st->cur ^= 1;
-    const double t = st->t + h;
-    st->t = t;
-    st->steps += 1;
-    st->numloops = 0;
-    const double hs = accept_h(s, h, ctl);
-    st->h_suggest = hs;
-    const double hn = (t + hs > st->tf) ? st->tf - t : hs;
-    st->h = hn;
-    if (!(t < st->tf)) st->status = RK_ST_DONE;
-    else if (t + hn == t) st->status = RK_ST_MIN_STEP;
+  if (tid == 0) {
+    for (int i = 0; i < ATTEMPT_THREADS / 32; ++i) {
+      m = fmin(m, wmin[i]);
+      nan |= wnan[i];
+    }
+    apply_controller(p, nan ? nan_d() : m);
+    *p.ctr = 0u;
+    __threadfence();
   }
 }
 
@@ -566,7 +635,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  if (tid == 0) {
+  if (tid == 0 || tid == 32) {
     int g = 0;
     const Ring ring{sm, full, empty};
     auto chunk = [&](int i) {
@@ -580,8 +649,12 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
       cc.first = i == 0;
       return cc;
     };
-    if (!run_chain(K / KC, chunk, g, ring, tmem, &tmA, &tmB)) atomicOr(error, 1);
-    tc::mma_commit(accb);
+    if (tid == 32) {
+      if (!chain_producer(K / KC, chunk, g, ring, &tmA, &tmB)) atomicOr(error, 1);
+    } else {
+      if (!chain_mma(K / KC, chunk, g, ring, tmem)) atomicOr(error, 1);
+      tc::mma_commit(accb);
+    }
   }
   const bool ok = tc::mbar_wait(accb, 0u, WAIT_NS);
   if (!ok) atomicOr(error, 2);
@@ -694,6 +767,8 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   p.Si = reinterpret_cast<const double*>(w + L.Si);
   p.shift = reinterpret_cast<const float*>(w + L.shift);
   p.s = reinterpret_cast<double*>(w + L.s);
+  p.cmin = reinterpret_cast<double*>(w + L.cmin);
+  p.ctr = reinterpret_cast<unsigned int*>(w + L.ctr);
   p.n_inst = b->n_inst;
   p.bpad = L.bpad;
   p.n = b->n;
@@ -711,10 +786,8 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   for (int64_t a = 0; a < b->max_attempts; a += per_check) {
     const int64_t r_end = a + per_check < b->max_attempts ? per_check : b->max_attempts - a;
     for (int64_t r = 0; r < r_end; ++r) {
-      coef_diag_kernel<<<1, 128, 0, s>>>(p);
-      coef_matrix_kernel<<<dim3(16, NCOEF), 256, 0, s>>>(p);
+      coef_kernel<<<dim3(16, NCOEF), 256, 0, s>>>(p);
       attempt_kernel<<<(unsigned)(L.bpad / NT), ATTEMPT_THREADS, ATTEMPT_SMEM, s>>>(tmA, tmV, p);
-      control_kernel<<<1, 1024, 0, s>>>(p);
     }
     if (int e = cuda_check(cudaGetLastError(), "dense attempt launch")) return e;
     if (int e = cuda_check(cudaMemcpyAsync(&hs, b->state, sizeof(hs), cudaMemcpyDeviceToHost, s), "state read")) return e;
