@@ -45,10 +45,17 @@ constexpr int A_TILE = DM * KC * 4;
 constexpr int B_TILE = NT * KC * 4;
 constexpr int SLOT_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr uint64_t WAIT_NS = 200000000ull;  // give up a wait after 200 ms
-constexpr int ATTEMPT_THREADS = 128;
+constexpr int GEMM_THREADS = 128;
+// attempt kernel: warps 0-3 epilogues (one tensor-memory lane quarter each), warp 4 issues
+// the MMAs, warp 5 the TMA loads
+constexpr int ATTEMPT_THREADS = 192;
+constexpr int MMA_TID = 128, PRODUCER_TID = 160;
 constexpr int ATTEMPT_SMEM = 1024 + NS * SLOT_BYTES + 256;
+constexpr int TMEM_COLS = 256;  // accumulator slots at columns 0 and NT, the error product at 2 NT
 
-enum { V_U0, V_U1, V_N1, V_N2, V_N3, V_N4, V_N5, V_N6, V_D23, V_D24, V_EV, NVEC };
+// N1 and N1B are N(u) of the state in U0 and U1: the last epilogue of an attempt writes
+// N(unew) next to unew, so an attempt starts with N1 ready
+enum { V_U0, V_U1, V_N1, V_N1B, V_N2, V_N3, V_N4, V_N5, V_N6, V_D23, V_D24, V_EV, NVEC };
 
 struct Layout {  // byte offsets into the work buffer
   int64_t bpad, a, v, cd, eig, S, Si, shift, s, cmin, ctr, total;
@@ -143,7 +150,9 @@ __global__ void load_u_kernel(Params p, const float* u) {
   const int64_t col = i / DM;
   const int row = (int)(i % DM);
   const float v = (col < p.n_inst && row < p.n) ? u[col * p.n + row] : 0.f;
-  vput(p, p.st->cur ? V_U1 : V_U0, col, row, v);
+  const int cur = p.st->cur;
+  vput(p, cur ? V_U1 : V_U0, col, row, v);
+  vput(p, cur ? V_N1B : V_N1, col, row, nl_ac(v, p.shift[row]));
 }
 
 __global__ void store_u_kernel(Params p, float* u) {
@@ -337,6 +346,15 @@ RK_DEV void apply_controller(const Params& p, double s) {
 // ---------------------------------------------------------------------------------
 // one ETD35 attempt for NT instances
 // ---------------------------------------------------------------------------------
+// rkstiff/etd35.py:690-719 as GEMM chains (coefficient matrix, vector, accumulator), the
+// terms that need the previous chain's epilogue last: while epilogue c runs on accumulator
+// slot c % 2, chain c + 1 accumulates its other terms in the other slot.
+struct ChainDef {
+  Term t[7];
+  int n;     // terms
+  int ndep;  // trailing terms that read the previous epilogue's outputs
+};
+
 __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     attempt_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmV, Params p) {
   rk_dense_state* st = p.st;
@@ -345,14 +363,16 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + NS * SLOT_BYTES);
   uint64_t* empty = full + NS;
-  uint64_t* accb = empty + NS;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* accb = empty + NS;  // chain c's accumulator complete (one phase per chain)
+  uint64_t* epi = accb + 1;     // [2] epilogue c done (outputs written, slot c % 2 read): epi[c % 2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(epi + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, row = tid;
   const int64_t col0 = (int64_t)blockIdx.x * NT;
   const int cur = st->cur;
   const int vU = cur ? V_U1 : V_U0, vUN = cur ? V_U0 : V_U1;
+  const int vN1 = cur ? V_N1B : V_N1, vN1N = cur ? V_N1 : V_N1B;
 
   if (tid == 0) {
     for (int i = 0; i < NS; ++i) {
@@ -360,6 +380,8 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
       tc::mbar_init(&empty[i], 1);
     }
     tc::mbar_init(accb, 1);
+    tc::mbar_init(&epi[0], 128);
+    tc::mbar_init(&epi[1], 128);
     *abort_flag = 0;
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tmA);
@@ -367,184 +389,208 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   }
   __syncwarp();
   if (warp == 0) {
-    tc::tmem_alloc(tmem_slot, 2 * NT);
+    tc::tmem_alloc(tmem_slot, TMEM_COLS);
     tc::tmem_relinquish();
   }
-  // N1 = N(u) (pointwise; thread = row).  ev accumulates the error combination
-  // -N1 + 4 N3 - 6 N4 + 4 N5 - N6 (etd35.py:344) in registers as the stages arrive, and
-  // n2 keeps N2 for N2 - N3 and N2 - 3 N4 / 2, so no epilogue reads a stage vector back.
-  const float xr = p.shift[row];
-  float ev[NT], n2[NT];
-#pragma unroll 16
-  for (int j = 0; j < NT; ++j) {
-    const float n1 = nl_ac(vget(p, vU, col0 + j, row), xr);
-    vput(p, V_N1, col0 + j, row, n1);
-    ev[j] = -n1;
-  }
-  tc::fence_proxy_async_global();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const Ring ring{sm, full, empty};
 
-  // rkstiff/etd35.py:690-719 as GEMM chains (coefficient matrix, vector, accumulator)
-  const Term chains[6][7] = {
-      {{C35_E14, vU, 0}, {C35_A21, V_N1, 0}},
-      {{C35_E14, vU, 0}, {C35_A31, V_N1, 0}, {C35_A32, V_N2, 0}},
-      {{C35_E12, vU, 0}, {C35_A41, V_N1, 0}, {C35_A43, V_N3, 0}},
-      {{C35_E34, vU, 0}, {C35_A51, V_N1, 0}, {C35_A52, V_D23, 0}, {C35_A54, V_N4, 0}},
-      {{C35_E, vU, 0}, {C35_A61, V_N1, 0}, {C35_A62, V_D24, 0}, {C35_A63, V_N3, 0}, {C35_A65, V_N5, 0}},
-      {{C35_E, vU, 0}, {C35_A71, V_N1, 0}, {C35_A73, V_N3, 0}, {C35_A74, V_N4, 0}, {C35_A75, V_N5, 0},
-       {C35_A76, V_N6, 0}, {C35_A75, V_EV, 1}}};
-  const int nterms[6] = {2, 3, 3, 4, 5, 7};
+  const ChainDef chains[6] = {
+      {{{C35_E14, vU, 0}, {C35_A21, vN1, 0}}, 2, 0},
+      {{{C35_E14, vU, 1}, {C35_A31, vN1, 1}, {C35_A32, V_N2, 1}}, 3, 1},
+      {{{C35_E12, vU, 0}, {C35_A41, vN1, 0}, {C35_A43, V_N3, 0}}, 3, 1},
+      {{{C35_E34, vU, 1}, {C35_A51, vN1, 1}, {C35_A52, V_D23, 1}, {C35_A54, V_N4, 1}}, 4, 1},
+      {{{C35_E, vU, 0}, {C35_A61, vN1, 0}, {C35_A62, V_D24, 0}, {C35_A63, V_N3, 0}, {C35_A65, V_N5, 0}}, 5, 1},
+      {{{C35_E, vU, 1}, {C35_A71, vN1, 1}, {C35_A73, V_N3, 1}, {C35_A74, V_N4, 1}, {C35_A75, V_N5, 1},
+        {C35_A76, V_N6, 1}, {C35_A75, V_EV, 2}},
+       7,
+       2}};
 
-  int g = 0;
-  float acc[32];
-  for (int ch = 0; ch < 6; ++ch) {
-    if (tid == 0 || tid == 32) {
-      const Term* terms = chains[ch];
-      const int64_t bpad = p.bpad;
-      auto chunk = [&](int i) {
-        const Term& t = terms[i >> 2];
-        ChunkCoord cc;
-        cc.k0 = (i & 3) * KC;
-        cc.a_hi = (t.coef * 2) * DM;
-        cc.a_lo = (t.coef * 2 + 1) * DM;
-        cc.b_hi = (int)((t.vec * 2) * bpad + col0);
-        cc.b_lo = (int)((t.vec * 2 + 1) * bpad + col0);
-        cc.acc = t.acc;
-        cc.first = (i & 3) == 0 && ((i >> 2) == 0 || terms[(i >> 2) - 1].acc != t.acc);
-        return cc;
-      };
-      const int nch = nterms[ch] * (DM / KC);
-      if (tid == 32) {
-        if (!*abort_flag && !chain_producer(nch, chunk, g, ring, &tmA, &tmV)) {
-          atomicOr(&st->error, 1);
-          *abort_flag = 1;
-        }
-      } else {
-        if (!*abort_flag && !chain_mma(nch, chunk, g, ring, tmem)) {
-          atomicOr(&st->error, 1);
-          *abort_flag = 1;
-        }
-        tc::mma_commit(accb);  // arrives once every MMA issued so far has completed
+  auto chunk_of = [&](const ChainDef& cd, int i) {
+    const Term& t = cd.t[i >> 2];
+    ChunkCoord cc;
+    cc.k0 = (i & 3) * KC;
+    cc.a_hi = (t.coef * 2) * DM;
+    cc.a_lo = (t.coef * 2 + 1) * DM;
+    cc.b_hi = (int)((t.vec * 2) * p.bpad + col0);
+    cc.b_lo = (int)((t.vec * 2 + 1) * p.bpad + col0);
+    cc.acc = t.acc;
+    cc.first = (i & 3) == 0 && ((i >> 2) == 0 || cd.t[(i >> 2) - 1].acc != t.acc);
+    return cc;
+  };
+
+  if (tid == PRODUCER_TID) {
+    // TMA loads of every chain, in order; a chain's trailing terms wait for the previous
+    // epilogue (its outputs are in global memory, fenced for the async proxy)
+    int g = 0;
+    for (int c = 0; c < 6 && !*abort_flag; ++c) {
+      const ChainDef& cd = chains[c];
+      const int nind = (cd.n - cd.ndep) * (DM / KC), nch = cd.n * (DM / KC);
+      auto ck = [&](int i) { return chunk_of(cd, i); };
+      int gi = g;
+      bool ok = chain_producer(nind, ck, gi, ring, &tmA, &tmV);
+      if (ok && c > 0) ok = tc::mbar_wait(&epi[(c - 1) & 1], (uint32_t)(((c - 1) >> 1) & 1), WAIT_NS);
+      if (ok) {
+        auto ckd = [&](int i) { return chunk_of(cd, nind + i); };
+        ok = chain_producer(nch - nind, ckd, gi, ring, &tmA, &tmV);
+      }
+      g = gi;
+      if (!ok) {
+        atomicOr(&st->error, 1);
+        *abort_flag = 1;
       }
     }
-    if (!tc::mbar_wait(accb, (uint32_t)ch & 1u, WAIT_NS)) {
-      atomicOr(&st->error, 2);
-      *abort_flag = 1;
+  } else if (tid == MMA_TID) {
+    int g = 0;
+    for (int c = 0; c < 6; ++c) {
+      const ChainDef& cd = chains[c];
+      const int nch = cd.n * (DM / KC);
+      bool ok = !*abort_flag;
+      // the slot this chain accumulates in was read by epilogue c - 2
+      if (ok && c >= 2) ok = tc::mbar_wait(&epi[c & 1], (uint32_t)(((c - 2) >> 1) & 1), WAIT_NS);
+      if (ok) {
+        tc::tc_fence_after();
+        auto ck = [&](int i) {
+          ChunkCoord cc = chunk_of(cd, i);
+          cc.acc = cd.t[i >> 2].acc == 2 ? 2 : (c & 1);
+          return cc;
+        };
+        ok = chain_mma(nch, ck, g, ring, tmem);
+      }
+      if (!ok) {
+        atomicOr(&st->error, 1);
+        *abort_flag = 1;
+      }
+      tc::mma_commit(accb);  // arrives once every MMA issued so far has completed
     }
-    tc::tc_fence_after();
-    __syncthreads();
-    if (*abort_flag) break;
-    if (ch < 5) {
+  } else if (warp < 4) {
+    // epilogues.  ev accumulates the error combination -N1 + 4 N3 - 6 N4 + 4 N5 - N6
+    // (etd35.py:344) as the stages arrive and n2 keeps N2 for N2 - N3 and N2 - 3 N4 / 2,
+    // so no epilogue reads a stage vector back.
+    const float xr = p.shift[row];
+    float ev[NT], n2[NT], acc[32];
+#pragma unroll 16
+    for (int j = 0; j < NT; ++j) ev[j] = -vget(p, vN1, col0 + j, row);
+    for (int c = 0; c < 6; ++c) {
+      if (!tc::mbar_wait(accb, (uint32_t)c & 1u, WAIT_NS)) {
+        atomicOr(&st->error, 2);
+        *abort_flag = 1;
+      }
+      if (*abort_flag) break;
+      tc::tc_fence_after();
+      const int slot = c & 1;
+      if (c < 5) {
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        load_acc_half(tmem, warp, 0, half, acc);
+        for (int half = 0; half < 2; ++half) {
+          load_acc_half(tmem, warp, slot, half, acc);
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          const int j = half * 32 + jj;
-          const int64_t c = col0 + j;
-          const float nk = nl_ac(acc[jj], xr);
-          if (ch == 0) {
-            vput(p, V_N2, c, row, nk);
-            n2[j] = nk;
-          } else if (ch == 1) {
-            vput(p, V_N3, c, row, nk);
-            vput(p, V_D23, c, row, n2[j] - nk);
-            ev[j] = ev[j] + 4.f * nk;
-          } else if (ch == 2) {
-            vput(p, V_N4, c, row, nk);
-            vput(p, V_D24, c, row, n2[j] - (3.f * nk) * 0.5f);
-            ev[j] = ev[j] - 6.f * nk;
-          } else if (ch == 3) {
-            vput(p, V_N5, c, row, nk);
-            ev[j] = ev[j] + 4.f * nk;
-          } else {
-            vput(p, V_N6, c, row, nk);
-            vput(p, V_EV, c, row, ev[j] - nk);
+          for (int jj = 0; jj < 32; ++jj) {
+            const int j = half * 32 + jj;
+            const int64_t col = col0 + j;
+            const float nk = nl_ac(acc[jj], xr);
+            if (c == 0) {
+              vput(p, V_N2, col, row, nk);
+              n2[j] = nk;
+            } else if (c == 1) {
+              vput(p, V_N3, col, row, nk);
+              vput(p, V_D23, col, row, n2[j] - nk);
+              ev[j] = ev[j] + 4.f * nk;
+            } else if (c == 2) {
+              vput(p, V_N4, col, row, nk);
+              vput(p, V_D24, col, row, n2[j] - (3.f * nk) * 0.5f);
+              ev[j] = ev[j] - 6.f * nk;
+            } else if (c == 3) {
+              vput(p, V_N5, col, row, nk);
+              ev[j] = ev[j] + 4.f * nk;
+            } else {
+              vput(p, V_N6, col, row, nk);
+              vput(p, V_EV, col, row, ev[j] - nk);
+            }
           }
         }
-      }
-      tc::fence_proxy_async_global();
-      tc::tc_fence_before();
-      __syncthreads();
-      tc::tc_fence_after();
-    } else {
-      // new state and the per-instance error test on it (solveras.py:412-455); the ring's
-      // shared memory is free: every MMA that read it has completed
-      constexpr int LD = NT + 1;
-      float* ru = reinterpret_cast<float*>(sm);
-      float* re = ru + DM * LD;
+        tc::fence_proxy_async_global();
+        tc::tc_fence_before();
+        tc::mbar_arrive(&epi[slot]);
+      } else {
+        // new state, N(unew) for the next attempt, and the per-instance error test on the
+        // new state (solveras.py:412-455).  The ring is idle: every chunk has been consumed.
+        constexpr int LD = NT + 1;
+        float* ru = reinterpret_cast<float*>(sm);
+        float* re = ru + DM * LD;
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        float err[32];
-        load_acc_half(tmem, warp, 0, half, acc);
-        load_acc_half(tmem, warp, 1, half, err);
+        for (int half = 0; half < 2; ++half) {
+          float err[32];
+          load_acc_half(tmem, warp, slot, half, acc);
+          load_acc_half(tmem, warp, 2, half, err);
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          const int j = half * 32 + jj;
-          vput(p, vUN, col0 + j, row, acc[jj]);
-          ru[row * LD + j] = acc[jj] * acc[jj];
-          re[row * LD + j] = err[jj] * err[jj];
+          for (int jj = 0; jj < 32; ++jj) {
+            const int j = half * 32 + jj;
+            vput(p, vUN, col0 + j, row, acc[jj]);
+            vput(p, vN1N, col0 + j, row, nl_ac(acc[jj], xr));
+            ru[row * LD + j] = acc[jj] * acc[jj];
+            re[row * LD + j] = err[jj] * err[jj];
+          }
         }
-      }
-      __syncthreads();
-      const int j = tid >> 1, half = tid & 1;
-      float mx = 0.f;
-      int nan = 0;
-      for (int r = 64 * half; r < 64 * half + 64; ++r) {
-        const float a2 = ru[r * LD + j];
-        if (a2 != a2) nan = 1;
-        else mx = fmaxf(mx, a2);
-      }
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-      nan |= __shfl_xor_sync(0xffffffffu, nan, 1);
-      const double maxu = nan ? nan_d() : (double)mx;
-      // NaN keeps every comparison false, as in the reference
-      const float thr = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff * maxu);
-      df au{0.f, 0.f}, ae{0.f, 0.f};
-      for (int r = 64 * half; r < 64 * half + 64; ++r) {
-        const float a2 = ru[r * LD + j];
-        if (a2 > thr) {
-          au = df_add(au, a2);
-          ae = df_add(ae, re[r * LD + j]);
+        tc::tc_fence_before();
+        tc::named_sync(1, 128);
+        const int j = tid >> 1, half = tid & 1;
+        float mx = 0.f;
+        int nan = 0;
+        for (int r = 64 * half; r < 64 * half + 64; ++r) {
+          const float a2 = ru[r * LD + j];
+          if (a2 != a2) nan = 1;
+          else mx = fmaxf(mx, a2);
         }
-      }
-      au = df_add(au, df{__shfl_xor_sync(0xffffffffu, au.hi, 1), __shfl_xor_sync(0xffffffffu, au.lo, 1)});
-      ae = df_add(ae, df{__shfl_xor_sync(0xffffffffu, ae.hi, 1), __shfl_xor_sync(0xffffffffu, ae.lo, 1)});
-      double s = INFINITY;  // padding columns do not take part
-      if (col0 + j < p.n_inst) {
-        const double su = (double)au.hi + (double)au.lo, se = (double)ae.hi + (double)ae.lo;
-        const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
-        if (ratio != ratio || isinf(ratio)) {
-          s = p.ctl.safety_f * ratio;
-        } else {
-          const float rf = (float)fmin(ratio, 1e30);
-          s = p.ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / 4.f));  // q = 4
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+        nan |= __shfl_xor_sync(0xffffffffu, nan, 1);
+        const double maxu = nan ? nan_d() : (double)mx;
+        // NaN keeps every comparison false, as in the reference
+        const float thr = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff * maxu);
+        df au{0.f, 0.f}, ae{0.f, 0.f};
+        for (int r = 64 * half; r < 64 * half + 64; ++r) {
+          const float a2 = ru[r * LD + j];
+          if (a2 > thr) {
+            au = df_add(au, a2);
+            ae = df_add(ae, re[r * LD + j]);
+          }
         }
-        if (half == 0) p.s[col0 + j] = s;
-      }
-      // the CTA's smallest s (NaN if any is NaN) for the batch controller
-      int snan = s != s;
-      double smin = snan ? INFINITY : s;
+        au = df_add(au, df{__shfl_xor_sync(0xffffffffu, au.hi, 1), __shfl_xor_sync(0xffffffffu, au.lo, 1)});
+        ae = df_add(ae, df{__shfl_xor_sync(0xffffffffu, ae.hi, 1), __shfl_xor_sync(0xffffffffu, ae.lo, 1)});
+        double sv = INFINITY;  // padding columns do not take part
+        if (col0 + j < p.n_inst) {
+          const double su = (double)au.hi + (double)au.lo, se = (double)ae.hi + (double)ae.lo;
+          const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
+          if (ratio != ratio || isinf(ratio)) {
+            sv = p.ctl.safety_f * ratio;
+          } else {
+            const float rf = (float)fmin(ratio, 1e30);
+            sv = p.ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / 4.f));  // q = 4
+          }
+          if (half == 0) p.s[col0 + j] = sv;
+        }
+        // the CTA's smallest s (NaN if any is NaN) for the batch controller
+        int snan = sv != sv;
+        double smin = snan ? INFINITY : sv;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) smin = fmin(smin, __shfl_xor_sync(0xffffffffu, smin, o));
-      snan = __any_sync(0xffffffffu, snan);
-      __shared__ double cm[4];
-      __shared__ int cn[4];
-      if ((tid & 31) == 0) {
-        cm[warp] = smin;
-        cn[warp] = snan;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        for (int i = 1; i < 4; ++i) {
-          smin = fmin(smin, cm[i]);
-          snan |= cn[i];
+        for (int o = 16; o > 0; o >>= 1) smin = fmin(smin, __shfl_xor_sync(0xffffffffu, smin, o));
+        snan = __any_sync(0xffffffffu, snan);
+        __shared__ double cm[4];
+        __shared__ int cn[4];
+        if ((tid & 31) == 0) {
+          cm[warp] = smin;
+          cn[warp] = snan;
         }
-        p.cmin[blockIdx.x] = snan ? nan_d() : smin;
+        tc::named_sync(1, 128);
+        if (tid == 0) {
+          for (int i = 1; i < 4; ++i) {
+            smin = fmin(smin, cm[i]);
+            snan |= cn[i];
+          }
+          p.cmin[blockIdx.x] = snan ? nan_d() : smin;
+        }
       }
     }
   }
@@ -554,7 +600,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   __syncwarp();
   if (warp == 0) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, 2 * NT);
+    tc::tmem_dealloc(tmem, TMEM_COLS);
   }
   // The last CTA to finish applies the lockstep controller to the batch's smallest s.
   // Every CTA read the state before incrementing the counter, so the update cannot race
@@ -567,14 +613,14 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   __syncthreads();
   if (!last) return;
   __threadfence();
-  __shared__ double wmin[4];
-  __shared__ int wnan[4];
+  __shared__ double wmin[ATTEMPT_THREADS / 32];
+  __shared__ int wnan[ATTEMPT_THREADS / 32];
   double m = INFINITY;
   int nan = 0;
   for (int i = tid; i < (int)gridDim.x; i += ATTEMPT_THREADS) {
-    const double s = __ldcg(p.cmin + i);
-    if (s != s) nan = 1;
-    else m = fmin(m, s);
+    const double sv = __ldcg(p.cmin + i);
+    if (sv != sv) nan = 1;
+    else m = fmin(m, sv);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -607,7 +653,7 @@ __global__ void split_kernel(const float* x, float* hi, float* lo, int64_t count
   lo[i] = v - h;
 }
 
-__global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, float* D, int K,
                 int N, int* error) {
   extern __shared__ unsigned char smem_raw[];
@@ -782,7 +828,7 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   load_u_kernel<<<(unsigned)((L.bpad * DM + 255) / 256), 256, 0, s>>>(p, b->u);
   if (int e = cuda_check(cudaGetLastError(), "dense set-up launch")) return e;
   rk_dense_state hs;
-  const int64_t per_check = 8;
+  const int64_t per_check = 32;  // attempts between host reads of the state (no-op launches past the end are cheap)
   for (int64_t a = 0; a < b->max_attempts; a += per_check) {
     const int64_t r_end = a + per_check < b->max_attempts ? per_check : b->max_attempts - a;
     for (int64_t r = 0; r < r_end; ++r) {
@@ -827,7 +873,7 @@ extern "C" int rk_tf32x3_gemm(const float* A, const float* B, float* D, int64_t 
   CUtensorMap tmA, tmB;
   if (int e = make_map(&tmA, Ahl, K, 2 * DM, DM)) return e;
   if (int e = make_map(&tmB, Bhl, K, 2 * N, NT)) return e;
-  gemm_kernel<<<(unsigned)(N / NT), ATTEMPT_THREADS, ATTEMPT_SMEM, s>>>(tmA, tmB, D, (int)K, (int)N, err);
+  gemm_kernel<<<(unsigned)(N / NT), GEMM_THREADS, ATTEMPT_SMEM, s>>>(tmA, tmB, D, (int)K, (int)N, err);
   if (int e = cuda_check(cudaGetLastError(), "gemm launch")) return e;
   int herr = 0;
   if (int e = cuda_check(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s), "error read")) return e;
