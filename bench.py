@@ -267,8 +267,10 @@ def forms_comparison(dev) -> dict:
     out = {"config": FORMS, "instances_finished_by_all": int(ok.sum())}
     for name, (st, dt, finals, ms) in runs.items():
         errs = np.array([np.linalg.norm(finals[i] - r) / np.linalg.norm(r) for i, r in zip(idx, ref)])
+        done = st["status"] == 0
         out[name] = {
             "mode_steps_per_s": float(np.sum(ms * st["steps"])) / dt,
+            "mode_time_units_per_s": float(np.sum(ms[done]) * FORMS["tf"]) / dt,
             "seconds": dt,
             "finished": int(np.sum(st["status"] == 0)),
             "nl_evals_per_unit_time": float(np.sum(st["nl_evals"][ok])) / (FORMS["tf"] * ok.sum()),

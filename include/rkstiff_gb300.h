@@ -295,7 +295,10 @@ typedef struct rk_dense_batch {
   int32_t n;             /* vector length, 1..RK_DENSE_NMAX                               */
   int64_t n_inst;        /* instances                                                     */
   int32_t nl_kind;       /* RK_NL_ALLEN_CAHN                                              */
-  int32_t reserved0;
+  int32_t err_eigen;     /* 0: error vector in physical space (etd35.py:719, the
+                            non-diagonal form); 1: in the eigenbasis, S^-1 applied, as the
+                            diagonalized form returns it (etd35.py:495) - the mask still
+                            comes from the physical state                                  */
   const double* eig;     /* [device] n real eigenvalues of lin_op                        */
   const double* S;       /* [device] n x n eigenvectors, row-major                       */
   const double* Sinv;    /* [device] n x n inverse of S, row-major                       */

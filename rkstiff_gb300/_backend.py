@@ -94,8 +94,12 @@ class DenseBackend:
             raise NotImplementedError(f"{method}: the dense (2-D lin_op) path implements ETD35")
         opts = solver.device_options
         self.solver = solver
+        # diagonalize=True: the error vector in the eigenbasis, as the reference's
+        # diagonalized ETD35 forms it (etd35.py:495); otherwise in physical space (etd35.py:719)
+        basis = "eigen" if getattr(solver, "diagonalize", False) else "physical"
         self.ens = DenseEnsemble(solver.lin_op, solver.nl_func, 1, config=getattr(solver, "config", None),
-                                 etd_config=getattr(solver, "etd_config", None), device=opts.device)
+                                 etd_config=getattr(solver, "etd_config", None), device=opts.device,
+                                 err_basis=basis)
         self.reset()
 
     def reset(self):

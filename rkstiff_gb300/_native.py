@@ -67,7 +67,7 @@ class RkTerm(ctypes.Structure):
 class RkDenseBatch(ctypes.Structure):
     _fields_ = [
         ("method", ctypes.c_int32), ("n", ctypes.c_int32), ("n_inst", ctypes.c_int64),
-        ("nl_kind", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("nl_kind", ctypes.c_int32), ("err_eigen", ctypes.c_int32),
         ("eig", ctypes.c_void_p), ("S", ctypes.c_void_p), ("Sinv", ctypes.c_void_p), ("shift", ctypes.c_void_p),
         ("u", ctypes.c_void_p), ("work", ctypes.c_void_p), ("state", ctypes.c_void_p),
         ("ctl", RkController), ("etd", RkEtdConfig), ("max_attempts", ctypes.c_int64),

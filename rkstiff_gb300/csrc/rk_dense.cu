@@ -41,6 +41,8 @@ constexpr int NT = RK_DENSE_TILE;  // instances per CTA = MMA N
 constexpr int KC = 32;             // K elements per pipeline chunk (128 bytes of FP32)
 constexpr int NS = 4;              // pipeline slots
 constexpr int NCOEF = C35_N;       // 21 coefficient matrices
+constexpr int C_ERR_EIG = NCOEF;   // diag(a75) S^-1: the error product in the eigenbasis
+constexpr int NMAT = NCOEF + 1;
 constexpr int A_TILE = DM * KC * 4;
 constexpr int B_TILE = NT * KC * 4;
 constexpr int SLOT_BYTES = 2 * A_TILE + 2 * B_TILE;
@@ -66,7 +68,7 @@ inline Layout layout(int64_t n_inst) {
   L.bpad = (n_inst + NT - 1) / NT * NT;
   int64_t o = 0;
   L.a = o;
-  o = al1k(o + (int64_t)NCOEF * 2 * DM * DM * 4);
+  o = al1k(o + (int64_t)NMAT * 2 * DM * DM * 4);
   L.v = o;
   o = al1k(o + (int64_t)NVEC * 2 * L.bpad * DM * 4);
   L.cd = o;
@@ -91,7 +93,7 @@ inline Layout layout(int64_t n_inst) {
 
 struct Params {
   rk_dense_state* st;
-  float* A;              // [NCOEF][2][DM][DM]
+  float* A;              // [NMAT][2][DM][DM]
   float* V;              // [NVEC][2][bpad][DM]
   double* Cd;            // [NCOEF][DM]
   const cx<double>* eig; // [DM]
@@ -103,6 +105,7 @@ struct Params {
   unsigned int* ctr;     // CTAs of the current attempt that have finished
   int64_t n_inst, bpad;
   int n;
+  int err_eigen;
   rk_controller ctl;
   EtdCfg ec;
 };
@@ -187,6 +190,18 @@ __global__ void __launch_bounds__(256) coef_kernel(Params p) {
   const int c = blockIdx.y;
   const int i0 = (blockIdx.x >> 2) * 32, j0 = (blockIdx.x & 3) * 32;
   const int r = tid >> 3, q0 = (tid & 7) * 4;
+  if (c == C_ERR_EIG) {
+    // row i of S^-1 scaled by a75(h lambda_i)
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int i = i0 + r, j = j0 + q0 + t;
+      const double v = Cd[C35_A75 * DM + i] * p.Si[i * DM + j];
+      const float hi = tc::tf32_hi((float)v);
+      p.A[(((int64_t)c * 2 + 0) * DM + i) * DM + j] = hi;
+      p.A[(((int64_t)c * 2 + 1) * DM + i) * DM + j] = (float)(v - (double)hi);
+    }
+    return;
+  }
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k0 = 0; k0 < DM; k0 += 32) {
     for (int e = tid; e < 32 * 32; e += 256) {
@@ -405,7 +420,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
       {{{C35_E34, vU, 1}, {C35_A51, vN1, 1}, {C35_A52, V_D23, 1}, {C35_A54, V_N4, 1}}, 4, 1},
       {{{C35_E, vU, 0}, {C35_A61, vN1, 0}, {C35_A62, V_D24, 0}, {C35_A63, V_N3, 0}, {C35_A65, V_N5, 0}}, 5, 1},
       {{{C35_E, vU, 1}, {C35_A71, vN1, 1}, {C35_A73, V_N3, 1}, {C35_A74, V_N4, 1}, {C35_A75, V_N5, 1},
-        {C35_A76, V_N6, 1}, {C35_A75, V_EV, 2}},
+        {C35_A76, V_N6, 1}, {p.err_eigen ? C_ERR_EIG : C35_A75, V_EV, 2}},
        7,
        2}};
 
@@ -818,10 +833,11 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   p.n_inst = b->n_inst;
   p.bpad = L.bpad;
   p.n = b->n;
+  p.err_eigen = b->err_eigen ? 1 : 0;
   p.ctl = b->ctl;
   p.ec = EtdCfg{b->etd.modecutoff, b->etd.contour_radius, b->etd.contour_points};
   CUtensorMap tmA, tmV;
-  if (int e = make_map(&tmA, p.A, DM, (int64_t)NCOEF * 2 * DM, DM)) return e;
+  if (int e = make_map(&tmA, p.A, DM, (int64_t)NMAT * 2 * DM, DM)) return e;
   if (int e = make_map(&tmV, p.V, DM, (int64_t)NVEC * 2 * L.bpad, NT)) return e;
   cudaStream_t s = (cudaStream_t)stream;
   pad_kernel<<<(DM * DM + 255) / 256, 256, 0, s>>>(p, b->eig, b->S, b->Sinv, b->shift);
@@ -832,7 +848,7 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   for (int64_t a = 0; a < b->max_attempts; a += per_check) {
     const int64_t r_end = a + per_check < b->max_attempts ? per_check : b->max_attempts - a;
     for (int64_t r = 0; r < r_end; ++r) {
-      coef_kernel<<<dim3(16, NCOEF), 256, 0, s>>>(p);
+      coef_kernel<<<dim3(16, NMAT), 256, 0, s>>>(p);
       attempt_kernel<<<(unsigned)(L.bpad / NT), ATTEMPT_THREADS, ATTEMPT_SMEM, s>>>(tmA, tmV, p);
     }
     if (int e = cuda_check(cudaGetLastError(), "dense attempt launch")) return e;

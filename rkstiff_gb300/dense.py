@@ -28,7 +28,15 @@ class DenseEnsemble:
     FP64 coefficient matrices, 3xTF32 stage products)."""
 
     def __init__(self, lin_op, nl_func: BuiltinNL, n_inst: int, config: Optional[SolverConfig] = None,
-                 etd_config: Optional[ETDConfig] = None, device=None, method: str = "ETD35"):
+                 etd_config: Optional[ETDConfig] = None, device=None, method: str = "ETD35",
+                 err_basis: str = "physical"):
+        """``err_basis``: "physical" forms the embedded error vector in physical space, as the
+        reference's non-diagonal ETD35 does (etd35.py:719); "eigen" forms it in the eigenbasis
+        (S^-1 applied) with the mask taken from the physical state, as the reference's
+        diagonalized ETD35 returns it (etd35.py:495)."""
+        if err_basis not in ("physical", "eigen"):
+            raise ValueError("err_basis must be 'physical' or 'eigen'")
+        self.err_eigen = 1 if err_basis == "eigen" else 0
         if method != "ETD35":
             raise NotImplementedError("the dense tensor-core path implements ETD35")
         if not isinstance(nl_func, BuiltinNL) or nl_func.kind != nat.RK_NL_ALLEN_CAHN:
@@ -107,6 +115,7 @@ class DenseEnsemble:
         b.n = self.n
         b.n_inst = self.n_inst
         b.nl_kind = nat.RK_NL_ALLEN_CAHN
+        b.err_eigen = self.err_eigen
         b.eig, b.S, b.Sinv, b.shift = (t.data_ptr() for t in (self.eig, self.S, self.Sinv, self.shift))
         b.u = u.data_ptr()
         b.work = self.work_ptr

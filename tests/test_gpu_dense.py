@@ -176,3 +176,29 @@ def test_solver_api_with_a_dense_operator():
     assert np.linalg.norm(np.asarray(uf).real - rf.real) <= 1e-4 * np.linalg.norm(rf.real)
     unew, h_used, h_next = solver.step(w0, 0.01)
     assert h_used == 0.01 and h_next > 0
+
+
+def test_diagonalized_error_semantics():
+    """diagonalize=True forms the error vector in the eigenbasis with the mask of the
+    physical state (etd35.py:495): the first attempt's s and the accept/reject sequence to
+    t=10 match the oracle's diagonalized ETD35, the reference's result for that form."""
+    from rkstiff_gb300 import ETD35
+
+    x, (lin, nl) = ac_ops(20)
+    xi = x[1:-1]
+    w0 = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi) - xi
+    ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4), err_basis="eigen")
+    u = ens.pack_u(w0[None, :])
+    ens.put_state(ens.fresh_state(0.0, 10.0, 0.05))
+    st = ens.run(u, 1)
+    o = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), diagonalize=True)
+    o.reset()
+    o.step(w0.astype(np.complex128), 0.05)
+    # FP32 stages leave the cancelling error combination ~1e-3 relative, s ~4e-4
+    assert abs(float(st["s_last"][0]) - o.log[0][2]) <= 2e-3 * o.log[0][2], (st["s_last"], o.log[0])
+    solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4), diagonalize=True)
+    uf = solver.evolve(w0, t0=0.0, tf=10.0, store_data=False)
+    ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), diagonalize=True)
+    rf = ref.evolve(w0.astype(np.complex128), 0.0, 10.0, store_data=False).real
+    assert abs(solver.stats["attempts"] - ref.attempts) <= 1, (solver.stats, ref.attempts)
+    assert np.linalg.norm(np.asarray(uf).real - rf) <= 5e-4 * np.linalg.norm(rf)
