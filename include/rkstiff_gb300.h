@@ -240,6 +240,10 @@ int rk_evolve_noalloc(const rk_batch* b, void* stream);
  *               complex per coef_complex in the same precision
  *   rk_error_s: *s_out = safety (eps |u[mask]| / |err[mask]|)^(1/q), the mask and norms of
  *               solveras.py:412-455, in FP64 on the device
+ *   rk_cgemv:   y = M x, M a dense n x n complex matrix (row-major) in the precision's
+ *               complex type, y not aliasing x: the basis changes S v and S^-1 N of a dense
+ *               lin_op stepped in its eigenbasis (the S.dot / Sinv.dot of the diagonalized
+ *               strategies, etd35.py:348-495, etd34.py:194-304, if34.py:137-199)
  * All pointers [device] except terms (host array) and ctl (host). */
 typedef struct rk_term {
   const void* coef;
@@ -250,6 +254,7 @@ int rk_combine(int32_t precision, int32_t coef_complex, int64_t m, const rk_term
                void* stream);
 int rk_error_s(int32_t precision, int64_t m, const void* unew, const void* err, const rk_controller* ctl, int32_t q,
                double* s_out, void* stream);
+int rk_cgemv(int32_t precision, int64_t n, const void* M, const void* x, void* y, void* stream);
 
 /* Learned step-size controller (no counterpart in the reference).  Training kernels on a
  * batch of `batch` samples X[batch][RK_MLP_IN] with targets T[batch], FP32:

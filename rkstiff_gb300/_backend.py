@@ -87,6 +87,16 @@ class DenseBackend:
     lin_op: ETD35 with FP64 psi-matrices and 3xTF32 tensor-core stages, FP32 states.  With a
     single instance the lockstep controller is the reference's controller."""
 
+    @staticmethod
+    def takes(solver) -> bool:
+        """ETD35, FP32, the built-in Allen-Cahn nonlinearity, n <= 128."""
+        from .models import BuiltinNL
+
+        nl = solver.nl_func
+        return (solver._method_name == "ETD35" and solver.device_options.precision == "fp32"
+                and isinstance(nl, BuiltinNL) and nl.kind == nat.RK_NL_ALLEN_CAHN
+                and tuple(solver.lin_op.shape)[0] <= nat.RK_DENSE_NMAX)
+
     def __init__(self, solver, method: str):
         from .dense import DenseEnsemble
 

@@ -1,4 +1,5 @@
-"""Execution backend for a user-supplied nonlinearity on a diagonal operator.
+"""Execution backends for a user-supplied nonlinearity: on a diagonal operator
+(``CallableBackend``) and on a dense one stepped in its eigenbasis (``EigenBackend``).
 
 The reference takes any callable ``nl_func`` (rkstiff/solver.py:104-115).  Here it must be a
 device-side torch callable: it receives the stage vector as a 1-D complex tensor on the
@@ -35,7 +36,8 @@ MAX_LOOPS, MAX_S, MIN_S = 50, 4.0, 0.25
 class CallableBackend:
     """One solver's device stepping loop around a torch nonlinearity (diagonal lin_op)."""
 
-    def __init__(self, solver, method: str):
+    def __init__(self, solver, method: str, lin=None):
+        """``lin``: the diagonal the coefficients are built from (default: solver.lin_op)."""
         nl = solver.nl_func
         if not callable(nl):
             raise TypeError("nl_func must be callable")
@@ -47,7 +49,7 @@ class CallableBackend:
         self.device = torch.device(opts.device) if opts.device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         self.prec = nat.RK_FP64 if opts.precision == "fp64" else nat.RK_FP32
-        lin = np.asarray(solver.lin_op)
+        lin = np.asarray(solver.lin_op if lin is None else lin)
         if lin.ndim != 1:
             raise NotImplementedError("the callable-nonlinearity path takes a diagonal (1-D) lin_op")
         self.m = int(lin.shape[0])
@@ -255,3 +257,57 @@ class CallableBackend:
         self.st["attempts"][0] += 1
         self.st["steps"][0] += 1
         return self._out(v, u), nat.RK_ST_RUNNING
+
+
+class EigenBackend(CallableBackend):
+    """A dense (2-D) lin_op with any method and nonlinearity, stepped in the eigenbasis of
+    lin_op = S diag(eig) S^-1 (eig and S^-1 once on the host in FP64, as the reference's
+    diagonalized strategies do: etd35.py:348-495, etd34.py:194-304, if34.py:137-199).
+
+    The state is v = S^-1 u; the coefficients are the diagonal ones of h eig (``rk_coeffs``),
+    each stage combination one ``rk_combine`` pass, each nonlinearity S^-1 N(S k) with the two
+    basis changes as ``rk_cgemv``.  The error test takes the physical state unew = S k and
+    either the eigenbasis error vector (``diagonalize=True``, the reference's diagonalized
+    result, etd35.py:495) or the physical one S err (``diagonalize=False``).  The second is the
+    reference's non-diagonal strategy (etd35.py:498-720, etd34.py:307-436, if34.py:202-254,
+    etd4.py:178-309, etd5.py:264-483, if4.py:125-199) in exact arithmetic: its psi-matrices
+    are S diag(psi(h eig)) S^-1, which this form applies without forming them (the reference
+    forms them by expm and a contour mean of resolvents)."""
+
+    def __init__(self, solver, method: str):
+        lin = solver.lin_op
+        lin = lin.detach().cpu().numpy() if isinstance(lin, torch.Tensor) else np.asarray(lin)
+        if lin.ndim != 2 or lin.shape[0] != lin.shape[1]:
+            raise ValueError("a 2-D lin_op must be square")
+        diagonalize = bool(getattr(solver, "diagonalize", False))
+        eig, S = np.linalg.eig(lin)
+        Sinv = np.linalg.inv(S)
+        self.cond_S = float(np.linalg.cond(S))
+        if not np.isfinite(self.cond_S) or self.cond_S > 1e12:
+            raise NotImplementedError(
+                f"lin_op's eigenvector matrix has condition number {self.cond_S:.3e}: the device path steps "
+                "in the eigenbasis and needs a diagonalizable operator")
+        super().__init__(solver, method, lin=eig)
+        self.n = int(lin.shape[0])
+        self.S = torch.as_tensor(np.ascontiguousarray(S, dtype=np.complex128), device=self.device).to(self.cdtype)
+        self.Sinv = torch.as_tensor(np.ascontiguousarray(Sinv, dtype=np.complex128), device=self.device).to(
+            self.cdtype)
+        self.err_physical = not diagonalize
+
+    def _mv(self, M, x):
+        y = torch.empty(self.n, dtype=self.cdtype, device=self.device)
+        nat.check(self.lib.rk_cgemv(self.prec, self.n, M.data_ptr(), x.data_ptr(), y.data_ptr(), self._stream()),
+                  "rk_cgemv")
+        return y
+
+    def _N(self, v):
+        return self._mv(self.Sinv, super()._N(self._mv(self.S, v)))
+
+    def _s(self, unew, err):
+        return super()._s(self._mv(self.S, unew), self._mv(self.S, err) if self.err_physical else err)
+
+    def _to_dev(self, u):
+        return self._mv(self.Sinv, super()._to_dev(u))
+
+    def _out(self, t, like):
+        return CallableBackend._out(self._mv(self.S, t), like)

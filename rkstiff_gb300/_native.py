@@ -98,7 +98,7 @@ assert STATE_DTYPE.itemsize == 128
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
-           "rk_combine", "rk_error_s")
+           "rk_combine", "rk_error_s", "rk_cgemv")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -158,6 +158,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_combine.restype = ctypes.c_int
         lib.rk_error_s.argtypes = [i32, i64, vp, vp, ctypes.POINTER(RkController), i32, vp, vp]
         lib.rk_error_s.restype = ctypes.c_int
+        lib.rk_cgemv.argtypes = [i32, i64, vp, vp, vp, vp]
+        lib.rk_cgemv.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

@@ -68,6 +68,29 @@ __global__ void error_s_kernel(const cx<T>* u, const cx<T>* e, int64_t m, rk_con
   }
 }
 
+// y = M x for a dense n x n complex matrix (row-major): one warp per row, lanes striding the
+// row (coalesced), warp-shuffle sum.  The basis changes S v and S^-1 N of the eigenbasis
+// stepping of a dense lin_op (the S.dot / Sinv.dot of etd35.py:377-495, if34.py:137-199)
+template <class T>
+__global__ void cgemv_kernel(const cx<T>* M, const cx<T>* x, cx<T>* y, int64_t n) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const cx<T>* r = M + row * n;
+  T ax = T(0), ay = T(0);
+  for (int64_t j = lane; j < n; j += 32) {
+    const cx<T> a = r[j], b = x[j];
+    ax += a.x * b.x - a.y * b.y;
+    ay += a.x * b.y + a.y * b.x;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ax += __shfl_xor_sync(0xffffffffu, ax, o);
+    ay += __shfl_xor_sync(0xffffffffu, ay, o);
+  }
+  if (lane == 0) y[row] = cx<T>{ax, ay};
+}
+
 }  // namespace callable
 }  // namespace rk
 
@@ -120,4 +143,21 @@ extern "C" int rk_error_s(int32_t precision, int64_t m, const void* unew, const 
     error_s_kernel<float><<<1, 1024, 0, s>>>(static_cast<const cx<float>*>(unew), static_cast<const cx<float>*>(err), m,
                                              *ctl, q, s_out);
   return cuda_check(cudaGetLastError(), "rk_error_s launch");
+}
+
+extern "C" int rk_cgemv(int32_t precision, int64_t n, const void* M, const void* x, void* y, void* stream) {
+  if (!M || !x || !y || n <= 0 || x == y || (precision != RK_FP64 && precision != RK_FP32)) {
+    set_error("rk_cgemv: invalid argument (y must not alias x)");
+    return RK_E_ARG;
+  }
+  const int rows_per_block = 8;
+  const unsigned blocks = (unsigned)((n + rows_per_block - 1) / rows_per_block);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == RK_FP64)
+    cgemv_kernel<double><<<blocks, 32 * rows_per_block, 0, s>>>(
+        static_cast<const cx<double>*>(M), static_cast<const cx<double>*>(x), static_cast<cx<double>*>(y), n);
+  else
+    cgemv_kernel<float><<<blocks, 32 * rows_per_block, 0, s>>>(
+        static_cast<const cx<float>*>(M), static_cast<const cx<float>*>(x), static_cast<cx<float>*>(y), n);
+  return cuda_check(cudaGetLastError(), "rk_cgemv launch");
 }

@@ -5,6 +5,7 @@ from __future__ import annotations
 from typing import Callable, Optional, Union
 
 from .etd import ETDAS, ETDConfig, SolverConfig
+from .solver import check_diagonalizable
 
 
 class ETD34(ETDAS):
@@ -17,6 +18,8 @@ class ETD34(ETDAS):
                  device_options=None) -> None:
         super().__init__(lin_op, nl_func, config, etd_config, loglevel=loglevel, device_options=device_options)
         self.diagonalize = bool(diagonalize)
+        if self.diagonalize and not self._diag:
+            check_diagonalizable(lin_op, self.logger)
         self._accept = False
 
     def _q(self) -> int:

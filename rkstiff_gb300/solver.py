@@ -19,6 +19,18 @@ def _shape(a):
     return np.shape(a)
 
 
+def check_diagonalizable(lin_op, logger) -> None:
+    """The diagonalized strategies' checks on a 2-D lin_op, made when the solver is built
+    (etd35.py:412-418, etd34.py:235-243, if34.py:157-163): ValueError when cond(lin_op) >
+    1e16, a warning above 1000."""
+    a = lin_op.detach().cpu().numpy() if isinstance(lin_op, torch.Tensor) else np.asarray(lin_op)
+    cond = np.linalg.cond(a)
+    if cond > 1e16:
+        raise ValueError("cannot diagonalize a non-invertible linear operator L")
+    if cond > 1000:
+        logger.warning(f"Linear matrix array has a large condition number of {cond:.2f}, method may be unstable")
+
+
 class BaseSolver(ABC):
     """Stores ``lin_op`` / ``nl_func``, validates the operator shape (1-D diagonal or
     square 2-D, rkstiff/solver.py:129-135) and keeps the ``t`` / ``u`` snapshot lists."""

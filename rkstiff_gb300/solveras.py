@@ -127,10 +127,15 @@ class BaseSolverAS(BaseSolver):
     def _engine(self):
         if self._backend is None:
             from ._backend import DenseBackend, DiagBackend
-            from ._callable import CallableBackend
+            from ._callable import CallableBackend, EigenBackend
             from .models import BuiltinNL
             if not self._diag:
-                self._backend = DenseBackend(self, self._method_name)
+                # FP32 ETD35 with the built-in Allen-Cahn nonlinearity: the tensor-core stages;
+                # any other dense problem: the eigenbasis stepping in the chosen precision
+                if DenseBackend.takes(self):
+                    self._backend = DenseBackend(self, self._method_name)
+                else:
+                    self._backend = EigenBackend(self, self._method_name)
             elif isinstance(self.nl_func, BuiltinNL):
                 self._backend = DiagBackend(self, self._method_name)
             else:

@@ -25,11 +25,11 @@ class BaseSolverCS(BaseSolver):
     def _engine(self):
         if self._backend is None:
             from ._backend import DiagBackend
-            from ._callable import CallableBackend
+            from ._callable import CallableBackend, EigenBackend
             from .models import BuiltinNL
             if not self._diag:
-                raise NotImplementedError(f"{type(self).__name__}: 2-D operators run ETD35 on the dense path")
-            if isinstance(self.nl_func, BuiltinNL):
+                self._backend = EigenBackend(self, self._method_name)
+            elif isinstance(self.nl_func, BuiltinNL):
                 self._backend = DiagBackend(self, self._method_name)
             else:
                 self._backend = CallableBackend(self, self._method_name)

@@ -61,6 +61,27 @@ def test_operator_shape_validation_and_types():
     assert s._diag and not rk.ETD35(np.eye(2), nl)._diag
 
 
+def test_dense_operator_checks_before_any_device_work(caplog):
+    """diagonalize=True checks cond(lin_op) when the solver is built, as the reference's
+    diagonalized strategies do (ValueError above 1e16, a warning above 1000); a defective
+    operator (a Jordan block) cannot be stepped in an eigenbasis and is refused with
+    NotImplementedError before anything touches the device."""
+    nl = lambda u: u  # noqa: E731
+    for cls in (rk.ETD35, rk.ETD34, rk.IF34):
+        with pytest.raises(ValueError):
+            cls(np.zeros((3, 3)), nl, diagonalize=True)
+    with caplog.at_level(logging.WARNING):
+        rk.ETD34(np.diag([1.0, 1e-4]), nl, diagonalize=True)
+    assert "condition number" in caplog.text
+    rk.ETD35(np.zeros(3), nl, diagonalize=True)  # 1-D: the diagonal strategy, no check
+    for s in (rk.ETD35(np.array([[-1.0, 1.0], [0.0, -1.0]]), nl), rk.IF4(np.array([[-1.0, 1.0], [0.0, -1.0]]), nl)):
+        with pytest.raises(NotImplementedError):
+            if s.solver_type == rk.SolverType.ADAPTIVE_STEP:
+                s.evolve(np.ones(2), 0.0, 1.0)
+            else:
+                s.evolve(np.ones(2), 0.0, 1.0, 0.1)
+
+
 def test_fresh_config_per_solver():
     nl = lambda u: u  # noqa: E731
     a = rk.ETD35(np.array([-1.0]), nl)

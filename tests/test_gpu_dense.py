@@ -21,6 +21,7 @@ from oracle import rk_oracle as O
 from rkstiff_gb300 import _native as nat
 from rkstiff_gb300 import models
 from rkstiff_gb300.dense import DenseEnsemble
+from rkstiff_gb300.device import DeviceOptions
 from rkstiff_gb300.solveras import SolverConfig
 import problems as P
 
@@ -156,7 +157,7 @@ def test_config5_batch_against_tight_fp64():
 
 
 def test_solver_api_with_a_dense_operator():
-    """ETD35(lin_op_2d, nl_func) runs the tensor-core path with the reference's snapshot
+    """ETD35(lin_op_2d, Allen-Cahn, precision fp32) runs the tensor-core path with the reference's snapshot
     semantics: a snapshot every store_freq accepted steps.  The error estimate cancels to
     ~1e-5 of the stage values, so FP32 stages move s (and the next h) by ~1e-3 relative:
     snapshot times agree to 5e-3, the final state at tf to 1e-4."""
@@ -165,8 +166,9 @@ def test_solver_api_with_a_dense_operator():
     x, (lin, nl) = ac_ops(20)
     xi = x[1:-1]
     w0 = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi) - xi
-    solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4))
+    solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4), device_options=DeviceOptions(precision="fp32"))
     uf = solver.evolve(w0, t0=0.0, tf=5.0, store_freq=3)
+    assert type(solver._engine()).__name__ == "DenseBackend"
     ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), dense_psi="eig")
     rf = ref.evolve(w0.astype(np.complex128), 0.0, 5.0, store_data=True, store_freq=3)
     assert len(solver.t) == len(ref.t) and solver.t[-1] == 5.0
@@ -196,7 +198,8 @@ def test_diagonalized_error_semantics():
     o.step(w0.astype(np.complex128), 0.05)
     # FP32 stages leave the cancelling error combination ~1e-3 relative, s ~4e-4
     assert abs(float(st["s_last"][0]) - o.log[0][2]) <= 2e-3 * o.log[0][2], (st["s_last"], o.log[0])
-    solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4), diagonalize=True)
+    solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4), diagonalize=True,
+                   device_options=DeviceOptions(precision="fp32"))
     uf = solver.evolve(w0, t0=0.0, tf=10.0, store_data=False)
     ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), diagonalize=True)
     rf = ref.evolve(w0.astype(np.complex128), 0.0, 10.0, store_data=False).real

@@ -1,0 +1,169 @@
+"""A dense (2-D) lin_op with any method and nonlinearity, stepped in its eigenbasis on the
+device, against the reference's own results (tests/golden/dense.npz: Allen-Cahn on 19
+Chebyshev interior points, made by the reference itself) and the oracle.
+
+Tolerances (FP64 unless stated):
+  * IF34 / IF4 (the reference forms expm matrices): 1e-10 / 1e-11 relative L2 against the
+    reference; the oracle's eigenbasis form of the same runs is 5e-14 / 7e-14 from it
+  * diagonalized ETD34 and IF34 (t=10): 1e-9 against the reference and its attempt count;
+    ETD35 to t=60 1e-7: the flow amplifies rounding there (a 1e-15 relative perturbation of
+    w0 moves the reference's own t=60 result by 0.8e-8 .. 3.3e-8)
+  * non-diagonal ETD4 (contour radius 10): the reference's contour mean of resolvents is
+    4.7e-7 from the exact psi-matrices, so 2e-6 against the reference and 1e-11 against the
+    oracle with exact (eigenbasis) psi-matrices
+  * non-diagonal ETD35 to t=60: 5e-5 against the reference (its contour error gives 1.0e-5
+    and one attempt more), 1e-7 against the oracle with exact psi-matrices (as above)
+  * snapshot times: rtol 1e-10 (s differs by rounding, and h follows s)
+  * ETD5: 1e-11 against the oracle with exact psi-matrices
+  * a complex, non-normal operator with a cubic (NLS-type) torch nonlinearity: IF34 1e-10
+    against the oracle's expm form, ETD35 1e-10 against its eigenbasis psi-matrices
+  * FP32 (complex64 stages and basis changes): one ETD35 step 2e-6 from the FP64 oracle
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import rkstiff_gb300 as rk
+from oracle import rk_oracle as O
+from rkstiff_gb300.device import DeviceOptions
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope="module")
+def ac(golden):
+    g = golden("dense")
+    x = g["cheb20_x"][1:-1]
+    xt = {}
+
+    def nl_torch(w):
+        key = (w.device, w.dtype)
+        if key not in xt:
+            xt[key] = torch.as_tensor(x, device=w.device).to(w.dtype)
+        xs = xt[key]
+        return xs - (w + xs) ** 3
+
+    def nl_np(w):
+        return x - (w + x) ** 3
+
+    return g, g["ac20_lin"], g["ac20_w0"], nl_torch, nl_np
+
+
+def test_backend_is_the_eigenbasis_path(ac):
+    g, lin, w0, nl_t, _ = ac
+    s = rk.IF34(lin, nl_t)
+    s.evolve(w0, 0.0, 0.1, store_data=False)
+    assert type(s._engine()).__name__ == "EigenBackend"
+
+
+@pytest.mark.parametrize("method,kw,tf,tol", [
+    ("IF34", {}, 10.0, 1e-10),
+    ("ETD35", {"diagonalize": True}, 60.0, 1e-7),
+    ("ETD34", {"diagonalize": True}, 10.0, 1e-9),
+    ("IF34", {"diagonalize": True}, 10.0, 1e-9),
+])
+def test_adaptive_dense_vs_reference(ac, method, kw, tf, tol):
+    g, lin, w0, nl_t, nl_np = ac
+    key = {("IF34", False): "ac20_IF34_dense_final", ("ETD35", True): "ac20_ETD35_diagz_final",
+           ("ETD34", True): "ac20_ETD34_diagz_final", ("IF34", True): "ac20_IF34_diagz_final"}[
+        (method, kw.get("diagonalize", False))]
+    s = getattr(rk, method)(lin, nl_t, config=rk.SolverConfig(epsilon=1e-4), **kw)
+    uf = s.evolve(w0, 0.0, tf, store_data=False)
+    o = O.OracleSolver(method, lin, nl_np, O.SolverConfig(epsilon=1e-4), dense_psi="eig", **kw)
+    o.evolve(w0.astype(np.complex128), 0.0, tf, store_data=False)
+    assert s.stats["attempts"] == o.attempts
+    assert rel(uf, g[key]) < tol
+
+
+def test_nondiagonal_etd35_vs_reference_and_exact_psi(ac):
+    g, lin, w0, nl_t, nl_np = ac
+    cfg = rk.ETDConfig(contour_points=32, contour_radius=10)
+    s = rk.ETD35(lin, nl_t, config=rk.SolverConfig(epsilon=1e-4), etd_config=cfg)
+    uf = s.evolve(w0, 0.0, 60.0, store_data=False)
+    assert rel(uf, g["ac20_ETD35_nondiag_final"]) < 5e-5
+    o = O.OracleSolver("ETD35", lin, nl_np, O.SolverConfig(epsilon=1e-4), O.ETDConfig(contour_points=32,
+                       contour_radius=10), dense_psi="eig")
+    ref = o.evolve(w0.astype(np.complex128), 0.0, 60.0, store_data=False)
+    assert s.stats["attempts"] == o.attempts
+    assert rel(uf, ref) < 1e-7
+
+
+@pytest.mark.parametrize("method,golden_key,tol_ref", [("IF4", "ac20_IF4_dense_final", 1e-11),
+                                                       ("ETD4", "ac20_ETD4_dense_final", 2e-6),
+                                                       ("ETD5", None, None)])
+def test_fixed_step_dense(ac, method, golden_key, tol_ref):
+    g, lin, w0, nl_t, nl_np = ac
+    cfg = rk.ETDConfig(contour_points=32, contour_radius=10)
+    kw = {} if method == "IF4" else {"etd_config": cfg}
+    s = getattr(rk, method)(lin, nl_t, **kw)
+    uf = s.evolve(w0, 0.0, 2.0, 0.01, store_data=False)
+    if golden_key is not None:
+        assert rel(uf, g[golden_key]) < tol_ref
+    okw = {} if method == "IF4" else {"etd_config": O.ETDConfig(contour_points=32, contour_radius=10)}
+    o = O.OracleSolver(method, lin, nl_np, dense_psi="eig", **okw)
+    ref = o.evolve(w0.astype(np.complex128), 0.0, 2.0, 0.01, store_data=False)
+    assert rel(uf, ref) < 1e-11
+
+
+def test_dense_snapshots_and_step(ac):
+    """store_freq snapshots (solveras.py:622-650) and the step API through the eigenbasis."""
+    g, lin, w0, nl_t, nl_np = ac
+    s = rk.ETD34(lin, nl_t, config=rk.SolverConfig(epsilon=1e-4))
+    s.evolve(w0, 0.0, 5.0, store_freq=2)
+    o = O.OracleSolver("ETD34", lin, nl_np, O.SolverConfig(epsilon=1e-4), dense_psi="eig")
+    o.evolve(w0.astype(np.complex128), 0.0, 5.0, store_data=True, store_freq=2)
+    assert len(s.t) == len(o.t)
+    np.testing.assert_allclose(s.t, o.t, rtol=1e-10)
+    for a, b in zip(s.u[1:], o.u[1:]):
+        assert rel(a, b) < 1e-10
+    unew, h_used, h_next = s.step(w0, 0.05)
+    on, oh, onext = O.OracleSolver("ETD34", lin, nl_np, O.SolverConfig(epsilon=1e-4), dense_psi="eig").step(
+        w0.astype(np.complex128), 0.05)
+    assert h_used == oh and abs(h_next - onext) <= 1e-12 * onext
+    assert rel(unew, on) < 1e-12
+
+
+def complex_operator(n=16, seed=3):
+    """A non-normal complex operator with a stable, complex spectrum: S diag(lam) S^-1, S a
+    well-conditioned random perturbation of I."""
+    rng = np.random.default_rng(seed)
+    S = np.eye(n) + 0.25 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+    lam = -rng.uniform(0.1, 20.0, n) + 1j * rng.uniform(-30.0, 30.0, n)
+    lin = S @ np.diag(lam) @ np.linalg.inv(S)
+    u0 = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    return lin, u0
+
+
+def test_complex_nonnormal_operator():
+    lin, u0 = complex_operator()
+
+    def nl_t(u):
+        return 1j * (u.abs() ** 2) * u
+
+    def nl_np(u):
+        return 1j * np.abs(u) ** 2 * u
+
+    for method, kw in (("IF34", {}), ("ETD35", {"dense_psi": "eig"})):
+        s = getattr(rk, method)(lin, nl_t, config=rk.SolverConfig(epsilon=1e-6))
+        uf = s.evolve(u0, 0.0, 1.0, store_data=False)
+        o = O.OracleSolver(method, lin, nl_np, O.SolverConfig(epsilon=1e-6), **kw)
+        ref = o.evolve(u0, 0.0, 1.0, store_data=False)
+        assert s.stats["attempts"] == o.attempts, method
+        assert rel(uf, ref) < 1e-10, method
+
+
+def test_fp32_dense_one_step(ac):
+    g, lin, w0, nl_t, nl_np = ac
+    s = rk.ETD35(lin, nl_t, config=rk.SolverConfig(epsilon=1e-4), device_options=DeviceOptions(precision="fp32"))
+    unew, h_used, _ = s.step(w0, 0.05)
+    assert type(s._engine()).__name__ == "EigenBackend"
+    o = O.OracleSolver("ETD35", lin, nl_np, O.SolverConfig(epsilon=1e-4), dense_psi="eig")
+    ref, h_ref, _ = o.step(w0.astype(np.complex128), 0.05)
+    assert h_used == h_ref
+    assert rel(unew, ref) < 2e-6
