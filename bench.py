@@ -416,10 +416,14 @@ def gpu_arm(args, rank, world, cpu_line):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
+    marks = [e0]
     for _ in range(args.steps):
         st = one_step()
         mode_steps += int(np.sum(eng.ms * st["steps"]))
         flops += flops_of(eng, st)
+        mark = torch.cuda.Event(enable_timing=True)
+        mark.record(stream)
+        marks.append(mark)
     e1.record(stream)
     torch.cuda.synchronize()
     if dist is not None:
@@ -468,6 +472,7 @@ def gpu_arm(args, rank, world, cpu_line):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": max_elapsed / args.steps * 1e3,
+        "step_ms": [round(a.elapsed_time(b), 3) for a, b in zip(marks[:-1], marks[1:])],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,

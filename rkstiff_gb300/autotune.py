@@ -1,10 +1,13 @@
 """Autotuner for the launch shape of each grid-size class of an ensemble.
 
 Each class (instances sharing one grid size) runs as its own kernel, concurrently with the
-other classes.  The tuner sweeps the classes in turn: for one class it times every
-candidate (threads per instance group, groups per block, scratch placement) while the
-other classes keep their current shapes, running a subsample of the whole ensemble over a
-short span of simulated time, and keeps the fastest.  Results are cached per (device,
+other classes.  The tuner takes the classes one at a time, each on its own: the class's
+instances (up to ``per_class`` of them) as a one-class ensemble, every candidate (threads
+per instance group, groups per block, scratch placement) timed over a short span of
+simulated time (best of ``reps`` + 1 runs), and keeps the candidate with the highest
+mode-steps/s.  Timing a class alone measures that class's kernel: in a mixed run the
+slowest class sets the wall time, so a trial of one class inside the mix cannot tell its
+candidates apart unless that class is the slowest.  Results are cached per (device,
 method, precision, operator kind, nonlinearity, grid-size mix) for the process and can be
 saved to / loaded from a JSON file.
 """
@@ -75,7 +78,7 @@ def _rate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, reps: int)
 
 
 def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequence], span: float,
-         h_init: Optional[float] = None, per_class: Optional[int] = None, reps: int = 1,
+         h_init: Optional[float] = None, per_class: Optional[int] = None, reps: int = 2,
          shapes: Sequence[Tuple[int, int]] = SHAPES, places: Sequence[int] = PLACES,
          force: bool = False) -> Dict[int, dict]:
     """Choose (threads, groups per block, placement) per class of ``eng`` and install them.
@@ -89,34 +92,31 @@ def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequ
         return {int(n): {"threads": c[0], "groups": c[1], "place": c[2], "cached": True}
                 for n, c in zip(eng.class_n, chosen)}
     nsm = torch.cuda.get_device_properties(eng.device).multi_processor_count
-    per_class = per_class or 2 * nsm
-    idx = []
-    for n in eng.class_n:
-        idx += [i for i in range(eng.n_inst) if eng.ns[i] == n][:per_class]
-    sub = DiagEnsemble(eng.method_name, [lin_ops[i] for i in idx], eng.nl_kind, eng.nl_coef,
-                       None if kxs is None else [kxs[i] for i in idx], [int(eng.ns[i]) for i in idx],
-                       precision="fp64" if eng.prec == nat.RK_FP64 else "fp32", device=eng.device,
-                       complex_operator=bool(eng.coef_complex))
-    sub.ctl, sub.etd = eng.ctl, eng.etd
-    u0 = sub.pack_u([u0s[i] for i in idx])
+    per_class = per_class or 8 * nsm
     h = h_init if h_init is not None else span / 100.0
-    assert list(sub.class_n) == list(eng.class_n)
-    chosen = [(128, 1, nat.RK_PLACE_GLOBAL)] * len(sub.class_n)
+    chosen = []
     report = {}
-    for c, n in enumerate(sub.class_n):
+    for n in eng.class_n:
+        idx = [i for i in range(eng.n_inst) if eng.ns[i] == n][:per_class]
+        sub = DiagEnsemble(eng.method_name, [lin_ops[i] for i in idx], eng.nl_kind, eng.nl_coef,
+                           None if kxs is None else [kxs[i] for i in idx], [int(eng.ns[i]) for i in idx],
+                           precision="fp64" if eng.prec == nat.RK_FP64 else "fp32", device=eng.device,
+                           complex_operator=bool(eng.coef_complex))
+        sub.ctl, sub.etd = eng.ctl, eng.etd
+        sub.mlp, sub.mlp_target = eng.mlp, eng.mlp_target
+        u0 = sub.pack_u([u0s[i] for i in idx])
         rates = {}
         for t, gr in shapes:
             for p in places:
-                trial = list(chosen)
-                trial[c] = (t, gr, p)
-                _install(sub, trial)
+                _install(sub, [(t, gr, p)])
                 r = _rate(sub, u0, span, h, reps)
                 if r is not None:
                     rates[(t, gr, p)] = r
         if not rates:
             raise RuntimeError(f"no launch shape fits grid size {n}")
-        chosen[c] = max(rates.items(), key=lambda kv: kv[1])[0]
-        report[int(n)] = {"threads": chosen[c][0], "groups": chosen[c][1], "place": chosen[c][2],
+        best = max(rates.items(), key=lambda kv: kv[1])[0]
+        chosen.append(best)
+        report[int(n)] = {"threads": best[0], "groups": best[1], "place": best[2],
                           "rates": {f"{a}x{b}/{p}": v for (a, b, p), v in rates.items()}}
     _CACHE[key] = tuple(chosen)
     _install(eng, chosen)
