@@ -51,3 +51,36 @@ def construct_x_dx_cheb(n: int, a: float = -1, b: float = 1) -> Tuple[np.ndarray
     D = np.outer(c, 1.0 / c) / (dX + np.eye(n + 1))
     D = D - np.diag(D.sum(axis=1))
     return x, D
+
+
+def construct_r_kr_hankel(nr: int, rmax: float) -> Tuple[np.ndarray, np.ndarray, np.ndarray, float]:
+    """Radial and spectral grids of the quasi-discrete Hankel transform of order zero
+    (rkstiff/grids.py:222-264): with j_1 .. j_{nr+1} the first zeros of J0,
+    r_i = j_i rmax / j_{nr+1} and kr_i = j_i / rmax.  Returns (r, kr, zeros, j_{nr+1})."""
+    from scipy import special
+
+    if nr < 4:
+        raise ValueError("nr must be >= 4.")
+    if rmax <= 0:
+        raise ValueError("rmax must be positive.")
+    z = special.jn_zeros(0, nr + 1)
+    zeros, jn = z[:-1], float(z[-1])
+    return zeros * rmax / jn, zeros / rmax, zeros, jn
+
+
+def mirror_grid(r: np.ndarray, u=None, axis: int = -1):
+    """Reflect a radial grid [0, rmax] (and values on it) to [-rmax, rmax]
+    (rkstiff/grids.py:267-321): the grid as -flip(r) followed by r; values flipped along
+    ``axis`` (-1: 1-D, 0: rows, 1: columns) and stacked in front."""
+    r = np.asarray(r)
+    rnew = np.concatenate([-r[::-1], r])
+    if u is None:
+        return rnew, None
+    u = np.asarray(u)
+    if axis == -1:  # rows flipped, stacked along the last axis of a 2-D array
+        return rnew, np.hstack([u[::-1], u])
+    if axis == 0:
+        return rnew, np.vstack([u[::-1], u])
+    if axis == 1:
+        return rnew, np.hstack([u[:, ::-1], u])
+    raise ValueError("axis must be -1, 0, or 1.")

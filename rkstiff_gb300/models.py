@@ -123,3 +123,63 @@ def kdv_multi_soliton(x: np.ndarray, ampl: Sequence[float], x0: Sequence[float],
     c = np.asarray(x0, dtype=float).reshape(1, -1)
     xx = np.asarray(x).reshape(-1, 1)
     return np.sum(0.5 * a**2 / (np.cosh(a * (xx - c - a**2 * t) / 2) ** 2), axis=1)
+
+
+# ---------------------------------------------------------------------------------------
+# multi-dimensional cubic NLS (the reference's NLS demo, demos/nls.ipynb): the state is the
+# flattened spectrum of a 2-D field, lin_op the flattened (diagonal) dispersion, and the
+# nonlinearity a device-side torch callable (the solvers' callable path) that reshapes,
+# transforms back, forms i gamma |F|^2 F and transforms forward.
+# ---------------------------------------------------------------------------------------
+class SpectralNL:
+    """A nonlinearity ``g -> fwd(i gamma |F|^2 F)`` with ``F = inv(g)`` on a flattened
+    spectrum; evaluated with torch on the input's device (numpy input: on the host, returned
+    as numpy)."""
+
+    def __init__(self, shape, inv, fwd, gamma: float, name: str):
+        self.shape, self._inv, self._fwd = tuple(shape), inv, fwd
+        self.gamma, self.name = float(gamma), name
+
+    def __call__(self, g):
+        if not isinstance(g, torch.Tensor):
+            return self(torch.from_numpy(np.asarray(g, dtype=np.complex128))).numpy()
+        F = self._inv(g.reshape(self.shape))
+        a2 = F.real * F.real + F.imag * F.imag
+        return self._fwd((1j * self.gamma) * (a2 * F)).reshape(-1)
+
+    def __repr__(self):
+        return f"SpectralNL({self.name}, shape={self.shape}, gamma={self.gamma})"
+
+
+def nls_radial_ops(ht, gamma: float = 2.0) -> Tuple[np.ndarray, SpectralNL]:
+    """Radially symmetric NLS on a Hankel grid (demos/nls.ipynb cells 6-12):
+    L = -i kr^2, N(g) = i gamma ht(|f|^2 f) with f = iht(g); ``ht`` a
+    ``transforms.HankelTransform`` (its transform runs as a GEMM on the device)."""
+    return -1j * ht.kr**2, SpectralNL((ht.nr,), ht.iht, ht.ht, gamma, "nls_radial")
+
+
+def nls_radial_time_ops(ht, omega: np.ndarray, sigma: float = 0.5,
+                        gamma: float = 2.0) -> Tuple[np.ndarray, SpectralNL]:
+    """(r, t) NLS with a Hankel transform over r (axis 0) and an FFT over t (axis 1)
+    (demos/nls.ipynb cells 14-20): L = -i kr^2 + i sigma omega^2 flattened row-major over
+    (nr, nt), N(g) = i gamma fft_t(ht(|F|^2 F)) with F = ifft_t(iht(g))."""
+    omega = np.asarray(omega, dtype=np.float64)
+    KR, OM = np.meshgrid(ht.kr, omega, indexing="ij")
+    L = (-1j * KR**2 + 1j * sigma * OM**2).reshape(-1)
+
+    def inv(G):
+        return torch.fft.ifft(ht.iht(G), dim=1)
+
+    def fwd(F):
+        return torch.fft.fft(ht.ht(F), dim=1)
+    return L, SpectralNL((ht.nr, len(omega)), inv, fwd, gamma, "nls_radial_time")
+
+
+def nls_2d_ops(kx: np.ndarray, ky: np.ndarray, gamma: float = 2.0) -> Tuple[np.ndarray, SpectralNL]:
+    """2-D NLS on complex FFT grids (demos/nls.ipynb cells 27-29): L = -i (kx^2 + ky^2)
+    flattened row-major over (nx, ny), N(g) = i gamma fft2(|F|^2 F) with F = ifft2(g)."""
+    kx = np.asarray(kx, dtype=np.float64)
+    ky = np.asarray(ky, dtype=np.float64)
+    KX, KY = np.meshgrid(kx, ky, indexing="ij")
+    L = (-1j * (KX**2 + KY**2)).reshape(-1)
+    return L, SpectralNL((len(kx), len(ky)), torch.fft.ifft2, torch.fft.fft2, gamma, "nls_2d")

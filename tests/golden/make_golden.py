@@ -310,13 +310,86 @@ def failure_cases(out):
             out["fail_burg"] = np.array(1)
 
 
+def multid_cases(out):
+    """The multi-dimensional spectral problems of the reference's NLS demo (demos/nls.ipynb):
+    the radial NLS on a Hankel grid, the (r, t) NLS with a Hankel transform in r and an FFT
+    in t, and the 2-D NLS with fft2; all ETD35 with a flattened diagonal lin_op.  Smaller
+    grids and horizons than the demo, the same operators and initial shapes."""
+    from rkstiff.transforms import HankelTransform
+    from rkstiff.grids import construct_x_kx_fft, mirror_grid
+    from rkstiff.etd35 import ETD35
+    from rkstiff.solveras import SolverConfig
+    gamma = 2.0
+    # the transform itself
+    HT = HankelTransform(nr=16, rmax=4.0)
+    out["ht16_r"], out["ht16_kr"] = HT.r, HT.kr
+    out["ht16_Y"], out["ht16_zeros"] = HT.hankel_matrix(), HT.bessel_zeros()
+    f = np.exp(-HT.r**2) * (1 + 0.5j * HT.r)
+    out["ht16_f"], out["ht16_ht"] = f, HT.ht(f)
+    out["ht16_iht"] = HT.iht(HT.ht(f))
+    rm, um = mirror_grid(HT.r, np.abs(f) ** 2)
+    out["ht16_mirror_r"], out["ht16_mirror_u"] = rm, um
+    # radial NLS (cells 6-12): L = -i kr^2, N = i gamma ht(|f|^2 f), f = iht(g)
+    HT = HankelTransform(nr=32, rmax=5.0)
+    L = -1j * HT.kr**2
+
+    def nl_r(g):
+        fr = HT.iht(g)
+        return 1j * gamma * HT.ht((fr.real**2 + fr.imag**2) * fr)
+    u0 = HT.ht(2.0 * np.exp(-HT.r**2))
+    s = ETD35(lin_op=L, nl_func=nl_r, config=SolverConfig(epsilon=1e-5))
+    out["hnls_u0"] = u0
+    out["hnls_final"] = s.evolve(u0, t0=0, tf=0.2, store_data=True, store_freq=5)
+    out["hnls_t"] = np.array(s.t)
+    # (r, t) NLS (cells 14-20): Hankel transform over axis 0, FFT over axis 1
+    nr, nt, sigma = 12, 32, 0.5
+    HT = HankelTransform(nr=nr, rmax=4.0)
+    t, omega = construct_x_kx_fft(nt, -6, 6)
+    R, T = np.meshgrid(HT.r, t, indexing="ij")
+    KR, OM = np.meshgrid(HT.kr, omega, indexing="ij")
+    L = (-1j * KR**2 + 1j * sigma * OM**2).flatten()
+
+    def nl_rt(g):
+        F = np.fft.ifft(HT.iht(g.reshape(nr, nt)), axis=1)
+        return 1j * gamma * np.fft.fft(HT.ht((F.real**2 + F.imag**2) * F), axis=1).flatten()
+    U0 = 4.0 * np.exp(-(R / 1.0) ** 2 - (T / 0.5) ** 2)
+    u0 = np.fft.fft(HT.ht(U0), axis=1).flatten()
+    s = ETD35(lin_op=L, nl_func=nl_rt, config=SolverConfig(epsilon=1e-5))
+    out["rtnls_u0"] = u0
+    out["rtnls_final"] = s.evolve(u0, t0=0, tf=0.03, store_data=False)
+    out["rtnls_shape"] = np.array([nr, nt])
+    # 2-D NLS (cells 27-29): fft2 on a 32 x 32 grid
+    nx = ny = 32
+    x, kx = construct_x_kx_fft(nx, -6, 6)
+    y, ky = construct_x_kx_fft(ny, -6, 6)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    KX, KY = np.meshgrid(kx, ky, indexing="ij")
+    L = (-1j * (KX**2 + KY**2)).flatten()
+
+    def nl_2d(g):
+        F = np.fft.ifft2(g.reshape(nx, ny))
+        return 1j * gamma * np.fft.fft2((F.real**2 + F.imag**2) * F).flatten()
+    u0 = np.fft.fft2(2.0 * np.exp(-X**2 - Y**2)).flatten()
+    s = ETD35(lin_op=L, nl_func=nl_2d)
+    out["nls2d_u0"] = u0
+    out["nls2d_final"] = s.evolve(u0, t0=0, tf=0.2, store_data=True, store_freq=4)
+    out["nls2d_t"] = np.array(s.t)
+
+
+CASES = (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases), ("adaptive", adaptive_cases),
+         ("controller", controller_cases), ("dense", dense_cases), ("failure", failure_cases),
+         ("multid", multid_cases))
+
+
 def main():
+    """make_golden.py [reference root] [case names...]: every case file by default."""
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    only = set(sys.argv[2:])
     tmp = import_reference(ref_root)
     try:
-        for fname, fn in (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases),
-                          ("adaptive", adaptive_cases), ("controller", controller_cases),
-                          ("dense", dense_cases), ("failure", failure_cases)):
+        for fname, fn in CASES:
+            if only and fname not in only:
+                continue
             out = {}
             fn(out)
             path = os.path.join(HERE, f"{fname}.npz")
