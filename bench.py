@@ -91,6 +91,20 @@ def _cpu_instance(args):
     return n // 2 + 1, steps, s.attempts, status
 
 
+def _cpu_dense_instance(args):
+    """One Allen-Cahn IC of the dense config by the oracle's diagonalized ETD35 (the
+    reference's eig-based form; its contour form costs tens of seconds per IC)."""
+    lin, shift, w0, eps, tf = args
+    from oracle import rk_oracle as O
+
+    def nl(v):
+        return shift - (v + shift) ** 3
+
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=eps), diagonalize=True)
+    s.evolve(w0.astype(np.complex128), 0.0, tf, store_data=False)
+    return sum(1 for r in s.log if r[3])
+
+
 def cpu_pool(cores: int):
     for var in ("OMP_NUM_THREADS", "MKL_NUM_THREADS", "OPENBLAS_NUM_THREADS"):
         os.environ[var] = "1"
@@ -345,6 +359,9 @@ def dense_measurement(dev) -> dict:
         "metric": "mode-steps/s",
         "value": 128.0 * DENSE["instances"] * st["steps"] / best,
         "seconds": best,
+        # ICs carried to tf per second: the fair comparison with a per-IC controller, which
+        # takes fewer steps than the lockstep batch (about 140 against 375 here)
+        "instances_per_s": DENSE["instances"] / best,
         "accepted_steps": st["steps"], "attempts": st["attempts"], "rejects": st["rejects"],
         "coefficient_updates": st["coeff_updates"],
         "rel_l2_vs_fp64_eps1e-8": errs,
@@ -357,7 +374,7 @@ def dense_measurement(dev) -> dict:
     }
 
 
-def gpu_arm(args, rank, world, cpu_line):
+def gpu_arm(args, rank, world, cpu_line, dense_cpu=None):
     import torch
 
     from rkstiff_gb300 import models, sharding
@@ -462,6 +479,8 @@ def gpu_arm(args, rank, world, cpu_line):
     peak = measure_fp32_peak(dev)
     forms = forms_comparison(dev) if (world == 1 and not args.no_forms) else None
     dense = dense_measurement(dev) if (world == 1 and not args.no_dense) else None
+    if dense is not None:
+        dense["cpu_baseline"] = dense_cpu
     achieved = flops / kernel_s / 1e12
     counts = {name: int(np.sum(status == code)) for name, code in (("done", 0), ("max_loops", 1), ("min_step", 2))}
     line = {
@@ -565,18 +584,34 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_line(cores: int):
+def cpu_baseline_line(cores: int, dense: bool = False):
+    """The KS ensemble's CPU baseline line and, with ``dense``, the dense config's (or None)."""
     inst = make_instances(WORKLOAD["instances"], WORKLOAD["seed"])
     sample = inst[: 4 * cores]
     pool = cpu_pool(cores)
+    dense_line = None
     try:
         value, wall, res = cpu_measure(pool, sample)
+        if dense:
+            from rkstiff_gb300 import workloads
+
+            lin, nl, w0 = workloads.allen_cahn_batch(4 * cores, DENSE["seed"], epsilon=DENSE["epsilon_ac"])
+            shift = np.asarray(nl.shift, dtype=np.float64)
+            t0 = time.perf_counter()
+            steps = pool.map(_cpu_dense_instance, [(lin, shift, w, DENSE["solver_epsilon"], DENSE["tf"]) for w in w0],
+                             chunksize=1)
+            dwall = time.perf_counter() - t0
+            dense_line = {"value": 128.0 * sum(steps) / dwall, "unit": "mode-steps/s", "cores": cores,
+                          "kind": "port", "instances_per_s": len(w0) / dwall,
+                          "sample": f"first {len(w0)} ICs of the dense config to tf={DENSE['tf']} by the NumPy FP64 "
+                                    f"oracle (diagonalized ETD35, per-IC controller), {cores} worker processes, "
+                                    f"{dwall:.1f} s wall"}
     finally:
         pool.close()
         pool.join()
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {len(sample)} instances of the workload to tf=100 by the NumPy FP64 oracle, "
-                      f"{cores} worker processes ({cpu_model()}), {wall:.1f} s wall"}
+    return ({"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+             "sample": f"first {len(sample)} instances of the workload to tf=100 by the NumPy FP64 oracle, "
+                       f"{cores} worker processes ({cpu_model()}), {wall:.1f} s wall"}, dense_line)
 
 
 def main():
@@ -603,16 +638,16 @@ def main():
         reference_arm(args, rank, world)
         return
     # the CPU baseline pool is spawned before any CUDA call
-    cpu_line = None
+    cpu_line = dense_cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu_line = cpu_baseline_line(host_cores())
+        cpu_line, dense_cpu = cpu_baseline_line(host_cores(), dense=not args.no_dense)
     if world > 1:
         import torch
         import torch.distributed as dist
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    gpu_arm(args, rank, world, cpu_line)
+    gpu_arm(args, rank, world, cpu_line, dense_cpu)
     if world > 1:
         import torch.distributed as dist
 
