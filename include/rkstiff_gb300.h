@@ -322,6 +322,43 @@ int64_t rk_dense_work_bytes(int64_t n_inst);
 /* Runs attempts until the state leaves RK_ST_RUNNING or max_attempts attempts ran; returns
  * after the stream has completed them (u holds the current states). */
 int rk_dense_evolve(const rk_dense_batch* b, void* stream);
+/* Dense lin_op path with a per-instance controller: every instance follows the reference's
+ * accept/reject rule with its own h (the rule of solveras.py:457-554 per instance, as a
+ * loop of single-instance solvers would), stepped in the eigenbasis of lin_op = S diag(eig)
+ * S^-1 as the reference's diagonalized ETD35 does (etd35.py:348-495): stage combinations
+ * elementwise with per-instance diagonal coefficients (rebuilt for an instance when its h
+ * changes), the basis changes S k and S^-1 N(S k) as 3xTF32 tensor-core GEMMs, one
+ * persistent launch per call.  Same operator limits as rk_dense_evolve (real spectrum,
+ * n <= RK_DENSE_NMAX, the Allen-Cahn nonlinearity).  The error vector is formed in
+ * physical space (err_eigen = 0, the non-diagonal form etd35.py:719) or in the eigenbasis
+ * (err_eigen = 1, etd35.py:495); the mask comes from the physical state either way. */
+typedef struct rk_dense_eig_batch {
+  int32_t method;        /* RK_ETD35                                                      */
+  int32_t n;             /* vector length, 1..RK_DENSE_NMAX                               */
+  int64_t n_inst;        /* instances                                                     */
+  int32_t nl_kind;       /* RK_NL_ALLEN_CAHN                                              */
+  int32_t err_eigen;     /* 0: physical error vector; 1: eigenbasis error vector          */
+  const double* eig;     /* [device] n real eigenvalues of lin_op                        */
+  const double* S;       /* [device] n x n eigenvectors, row-major                       */
+  const double* Sinv;    /* [device] n x n inverse of S, row-major                       */
+  const double* shift;   /* [device] n points x of the nonlinearity                      */
+  float* u;              /* [device] n_inst x n physical states, instance-major: read when
+                            first = 1, written by every call                              */
+  void* work;            /* [device] rk_dense_eig_work_bytes(n_inst) bytes, 1024-byte
+                            aligned; holds the eigenbasis state between calls            */
+  rk_inst_state* state;  /* [device] n_inst records: t, tf, h, h_coeff = NaN, status =
+                            RK_ST_RUNNING, zero counters and reserved_i (attempts since the
+                            last accepted step) before the first call                    */
+  rk_controller ctl;
+  rk_etd_config etd;
+  int32_t first;         /* 1: start from u (and set up the work buffer); 0: continue      */
+  int32_t max_attempts;  /* attempts each running instance may make in this call          */
+} rk_dense_eig_batch;
+int64_t rk_dense_eig_work_bytes(int64_t n_inst);
+/* Runs until every instance has left RK_ST_RUNNING or made max_attempts attempts; returns
+ * after the stream has completed them.  RK_E_CUDA if a device wait timed out. */
+int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream);
+
 /* The 3xTF32 tensor-core product of the dense path on its own (no counterpart in the
  * reference; a check of the GEMM): D[N][128] = B[N][K] * A[128][K]^T, FP32, K a multiple of
  * 32, N a multiple of RK_DENSE_TILE; work holds rk_tf32x3_work_bytes(K, N) bytes. */

@@ -23,6 +23,7 @@ RK_NL_NONE, RK_NL_UUX, RK_NL_NLS, RK_NL_ALLEN_CAHN = 0, 1, 2, 3
 RK_RUN_EVOLVE, RK_RUN_STEP = 0, 1
 RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
 RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE = 4, 5, 6
+RK_OK, RK_E_ARG, RK_E_CUDA, RK_E_UNSUPPORTED, RK_E_SIZE = 0, -1, -2, -3, -4
 RK_TW_N = 8192
 RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL = -1, 0, 1, 2
 
@@ -74,6 +75,16 @@ class RkDenseBatch(ctypes.Structure):
     ]
 
 
+class RkDenseEigBatch(ctypes.Structure):
+    _fields_ = [
+        ("method", ctypes.c_int32), ("n", ctypes.c_int32), ("n_inst", ctypes.c_int64),
+        ("nl_kind", ctypes.c_int32), ("err_eigen", ctypes.c_int32),
+        ("eig", ctypes.c_void_p), ("S", ctypes.c_void_p), ("Sinv", ctypes.c_void_p), ("shift", ctypes.c_void_p),
+        ("u", ctypes.c_void_p), ("work", ctypes.c_void_p), ("state", ctypes.c_void_p),
+        ("ctl", RkController), ("etd", RkEtdConfig), ("first", ctypes.c_int32), ("max_attempts", ctypes.c_int32),
+    ]
+
+
 RK_DENSE_NMAX, RK_DENSE_TILE = 128, 64
 # rk_dense_state (128 bytes)
 DENSE_STATE_DTYPE = np.dtype([
@@ -98,7 +109,7 @@ assert STATE_DTYPE.itemsize == 128
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
-           "rk_combine", "rk_error_s", "rk_cgemv")
+           "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -148,6 +159,10 @@ def load(build: bool = True) -> ctypes.CDLL:
             fn.restype = ctypes.c_int
         lib.rk_dense_work_bytes.argtypes = [i64]
         lib.rk_dense_work_bytes.restype = i64
+        lib.rk_dense_eig_work_bytes.argtypes = [i64]
+        lib.rk_dense_eig_work_bytes.restype = i64
+        lib.rk_dense_eig_evolve.argtypes = [ctypes.POINTER(RkDenseEigBatch), vp]
+        lib.rk_dense_eig_evolve.restype = ctypes.c_int
         lib.rk_dense_evolve.argtypes = [ctypes.POINTER(RkDenseBatch), vp]
         lib.rk_dense_evolve.restype = ctypes.c_int
         lib.rk_tf32x3_work_bytes.argtypes = [i64, i64]

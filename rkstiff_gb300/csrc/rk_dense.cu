@@ -784,6 +784,11 @@ int set_smem_attr() {
 }
 
 }  // namespace dense
+
+int make_tmap_f32_sw128(void* map, const void* base, int64_t inner, int64_t rows, int box_rows) {
+  return dense::make_map(static_cast<CUtensorMap*>(map), base, inner, rows, box_rows);
+}
+
 }  // namespace rk
 
 using namespace rk;

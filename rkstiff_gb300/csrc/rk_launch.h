@@ -40,6 +40,10 @@ RK_DECLARE_METHOD(ETD4)
 RK_DECLARE_METHOD(ETD5)
 RK_DECLARE_METHOD(IF4)
 
+// Tensor map of a rows x inner FP32 row-major array for TMA 2-D tile loads: box of 32
+// (inner) x box_rows, 128-byte swizzle (rk_dense.cu); `map` is a CUtensorMap.
+int make_tmap_f32_sw128(void* map, const void* base, int64_t inner, int64_t rows, int box_rows);
+
 // compile-time-size ETD35 kernels for real operators (rk_m_etd35_ct.cu); returns
 // RK_E_UNSUPPORTED when no specialisation exists for (precision, n)
 int launch_evolve_etd35_ct(const rk_batch& b, const ClassLaunch& c, cudaStream_t s);

@@ -29,13 +29,21 @@ class DenseEnsemble:
 
     def __init__(self, lin_op, nl_func: BuiltinNL, n_inst: int, config: Optional[SolverConfig] = None,
                  etd_config: Optional[ETDConfig] = None, device=None, method: str = "ETD35",
-                 err_basis: str = "physical"):
+                 err_basis: str = "physical", controller: str = "lockstep"):
         """``err_basis``: "physical" forms the embedded error vector in physical space, as the
         reference's non-diagonal ETD35 does (etd35.py:719); "eigen" forms it in the eigenbasis
         (S^-1 applied) with the mask taken from the physical state, as the reference's
-        diagonalized ETD35 returns it (etd35.py:495)."""
+        diagonalized ETD35 returns it (etd35.py:495).
+
+        ``controller``: "lockstep" (one h for the batch, ``rk_dense_evolve``: psi-matrices and
+        one K-concatenated GEMM per stage) or "instance" (every instance under the reference's
+        controller with its own h, ``rk_dense_eig_evolve``: the stages in the eigenbasis with
+        per-instance diagonal coefficients, the basis changes as GEMMs)."""
         if err_basis not in ("physical", "eigen"):
             raise ValueError("err_basis must be 'physical' or 'eigen'")
+        if controller not in ("lockstep", "instance"):
+            raise ValueError("controller must be 'lockstep' or 'instance'")
+        self.controller = controller
         self.err_eigen = 1 if err_basis == "eigen" else 0
         if method != "ETD35":
             raise NotImplementedError("the dense tensor-core path implements ETD35")
@@ -71,27 +79,36 @@ class DenseEnsemble:
         self.S = torch.as_tensor(S, dtype=torch.float64, device=dev).contiguous()
         self.Sinv = torch.as_tensor(Sinv, dtype=torch.float64, device=dev).contiguous()
         self.shift = torch.as_tensor(nl_func.shift, dtype=torch.float64, device=dev).contiguous()
-        nbytes = int(self.lib.rk_dense_work_bytes(self.n_inst))
+        per_instance = controller == "instance"
+        nbytes = int(self.lib.rk_dense_eig_work_bytes(self.n_inst) if per_instance
+                     else self.lib.rk_dense_work_bytes(self.n_inst))
         # torch's caching allocator returns 512-byte aligned blocks: over-allocate and align
         self._work_buf = torch.empty(nbytes + 1024, dtype=torch.uint8, device=dev)
         base = self._work_buf.data_ptr()
         self.work_ptr = (base + 1023) & ~1023
-        self.state_dev = torch.zeros(nat.DENSE_STATE_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        self.state_dtype = nat.STATE_DTYPE if per_instance else nat.DENSE_STATE_DTYPE
+        self.state_dev = torch.zeros(self.state_dtype.itemsize * (self.n_inst if per_instance else 1),
+                                     dtype=torch.uint8, device=dev)
         self.state = None
+        self._first = True
 
     # -- state ------------------------------------------------------------------------
     def fresh_state(self, t0: float, tf: float, h: float) -> np.ndarray:
-        st = np.zeros(1, dtype=nat.DENSE_STATE_DTYPE)
+        """Records of a run from t0 (one for the lockstep batch, one per instance otherwise)."""
+        st = np.zeros(self.n_inst if self.controller == "instance" else 1, dtype=self.state_dtype)
         st["t"], st["tf"], st["h"], st["h_coeff"] = t0, tf, h, np.nan
         st["status"] = nat.RK_ST_RUNNING
-        st["n1_fresh"] = 1
+        if self.controller == "lockstep":
+            st["n1_fresh"] = 1
         return st
 
     def put_state(self, st: np.ndarray) -> None:
-        self.state_dev.copy_(torch.from_numpy(st.view(np.uint8).copy()))
+        """Install records; the next run starts from the states in ``u``."""
+        self.state_dev.copy_(torch.from_numpy(np.ascontiguousarray(st).view(np.uint8).copy()))
+        self._first = True
 
     def get_state(self) -> np.ndarray:
-        return self.state_dev.cpu().numpy().view(nat.DENSE_STATE_DTYPE).copy()
+        return self.state_dev.cpu().numpy().view(self.state_dtype).copy()
 
     def pack_u(self, u0s) -> torch.Tensor:
         """(n_inst, n) FP32 device states from host arrays or tensors."""
@@ -107,10 +124,12 @@ class DenseEnsemble:
 
     # -- run --------------------------------------------------------------------------
     def run(self, u: torch.Tensor, max_attempts: int) -> np.ndarray:
-        """Continue the current state for at most ``max_attempts`` attempts; u in place."""
+        """Continue the current state for at most ``max_attempts`` attempts (per instance with
+        the instance controller); u in place."""
         if u.dtype != torch.float32 or u.device != self.device or not u.is_contiguous() or u.numel() != self.n_inst * self.n:
             raise ValueError("u must be a contiguous FP32 (n_inst, n) tensor on the ensemble's device")
-        b = nat.RkDenseBatch()
+        per_instance = self.controller == "instance"
+        b = nat.RkDenseEigBatch() if per_instance else nat.RkDenseBatch()
         b.method = nat.RK_ETD35
         b.n = self.n
         b.n_inst = self.n_inst
@@ -124,11 +143,19 @@ class DenseEnsemble:
         b.ctl = nat.RkController(c.epsilon, c.incr_f, c.decr_f, c.safety_f, c.adapt_cutoff, c.minh)
         e = self.etd_config
         b.etd = nat.RkEtdConfig(e.modecutoff, e.contour_radius, e.contour_points, 0)
-        b.max_attempts = int(max_attempts)
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
-            nat.check(self.lib.rk_dense_evolve(ctypes.byref(b), stream.cuda_stream), "rk_dense_evolve")
+            if per_instance:
+                b.first = 1 if self._first else 0
+                b.max_attempts = int(min(max_attempts, 2**31 - 1))
+                nat.check(self.lib.rk_dense_eig_evolve(ctypes.byref(b), stream.cuda_stream), "rk_dense_eig_evolve")
+                self._first = False
+            else:
+                b.max_attempts = int(max_attempts)
+                nat.check(self.lib.rk_dense_evolve(ctypes.byref(b), stream.cuda_stream), "rk_dense_evolve")
         self.state = self.get_state()
+        if per_instance and np.any(self.state["status"] == nat.RK_E_CUDA):
+            raise nat.NativeError("rk_dense_eig_evolve: a device wait timed out")
         return self.state
 
     def evolve(self, u0s, t0: float, tf: float, h_init: Optional[float] = None,
@@ -140,17 +167,23 @@ class DenseEnsemble:
         u = self.pack_u(u0s)
         self.put_state(self.fresh_state(t0, tf, h))
         st = self.run(u, max_attempts)
-        status = int(st["status"][0])
-        if status == nat.RK_ST_RUNNING:
+        if np.any(st["status"] == nat.RK_ST_RUNNING):
             raise RuntimeError(f"dense evolve did not reach tf within {max_attempts} attempts")
         return u
 
     def stats(self) -> dict:
+        """Counters of the last run: scalars for the lockstep batch; for the instance
+        controller the per-instance arrays plus their totals (``*_total``)."""
         st = self.state
         if st is None:
             raise RuntimeError("no evolve has run yet")
-        return {k: st[k][0].item() for k in ("t", "h", "status", "steps", "attempts", "rejects", "nl_evals",
-                                              "coeff_updates")}
+        keys = ("t", "h", "status", "steps", "attempts", "rejects", "nl_evals", "coeff_updates")
+        if self.controller == "lockstep":
+            return {k: st[k][0].item() for k in keys}
+        out = {k: st[k].copy() for k in keys}
+        for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates"):
+            out[k + "_total"] = int(st[k].sum())
+        return out
 
 
 def _main(argv=None) -> None:
@@ -167,14 +200,19 @@ def _main(argv=None) -> None:
     ap.add_argument("--tf", type=float, default=70.0)
     ap.add_argument("--epsilon", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--controller", choices=["lockstep", "instance"], default="lockstep")
     args = ap.parse_args(argv)
     lin, nl, w0 = workloads.allen_cahn_batch(args.instances, args.seed)
-    ens = DenseEnsemble(lin, nl, args.instances, config=SolverConfig(epsilon=args.epsilon))
+    ens = DenseEnsemble(lin, nl, args.instances, config=SolverConfig(epsilon=args.epsilon),
+                        controller=args.controller)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ens.evolve(w0, 0.0, args.tf)
     torch.cuda.synchronize()
     st = ens.stats()
+    if args.controller == "instance":
+        st = {k: v for k, v in st.items() if k.endswith("_total")}
+        st["status_max"] = int(ens.state["status"].max())
     st["seconds"] = time.perf_counter() - t0
     print(json.dumps(st))
 

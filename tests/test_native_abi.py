@@ -118,3 +118,22 @@ def test_dense_struct_layout_matches_c():
     for f, o in zip(nat.DENSE_STATE_DTYPE.names, soffs):
         assert nat.DENSE_STATE_DTYPE.fields[f][1] == o, f
     assert vals[-3:] == [nat.RK_DENSE_NMAX, nat.RK_DENSE_TILE, nat.RK_NL_ALLEN_CAHN]
+
+
+def test_dense_eig_struct_layout_matches_c():
+    """rk_dense_eig_batch offsets from the header against the ctypes view."""
+    fields = [f for f, _ in nat.RkDenseEigBatch._fields_]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void){",
+             'printf("%zu\\n", sizeof(rk_dense_eig_batch));']
+    for f in fields:
+        lines.append(f'printf("%zu\\n", offsetof(rk_dense_eig_batch, {f}));')
+    lines.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "probe.c")
+        exe = os.path.join(d, "probe")
+        open(c, "w").write("\n".join(lines))
+        subprocess.run(["gcc", "-O0", c, "-o", exe], check=True)
+        vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(nat.RkDenseEigBatch)
+    for f, o in zip(fields, vals[1:]):
+        assert getattr(nat.RkDenseEigBatch, f).offset == o, f
