@@ -83,9 +83,9 @@ class DiagBackend:
 
 
 class DenseBackend:
-    """One-instance dense ensemble (rkstiff_gb300.dense) behind a solver object with a 2-D
-    lin_op: ETD35 with FP64 psi-matrices and 3xTF32 tensor-core stages, FP32 states.  With a
-    single instance the lockstep controller is the reference's controller."""
+    """One-instance dense ensemble (rkstiff_gb300.dense, per-instance controller) behind a
+    solver object with a 2-D lin_op: ETD35 stepped in the eigenbasis with FP32 states and
+    3xTF32 tensor-core basis changes, under the reference's controller."""
 
     @staticmethod
     def takes(solver) -> bool:

@@ -251,7 +251,9 @@ RK_DEV int control_instance(rk_inst_state& s, double sv, const rk_controller& ct
 // start, decision a + 1 after attempt a's error test: continue or stop, in flags[0]).
 __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__ CUtensorMap tmA, Params p) {
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  // 1024-byte aligned by pointer arithmetic on the shared array (not through an integer),
+  // so that the compiler knows every pointer below addresses shared memory
+  unsigned char* sm = smem_raw + ((1024u - (uint32_t)(reinterpret_cast<uintptr_t>(smem_raw) & 1023u)) & 1023u);
   float* dep = reinterpret_cast<float*>(sm + NS * SLOT_BYTES);
   float* red = reinterpret_cast<float*>(sm + NS * SLOT_BYTES + DEP_BYTES);  // [3][4 warps][NT]
   unsigned char* ctl_area = sm + NS * SLOT_BYTES + DEP_BYTES + RED_BYTES;

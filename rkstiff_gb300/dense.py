@@ -2,11 +2,18 @@
 share one n x n lin_op (n <= 128), e.g. the Allen-Cahn Chebyshev operator.
 
 The operator is diagonalised once on the host in FP64 (lin_op = S diag(eig) S^-1, real
-spectrum; rkstiff/etd35.py:412-420 does the same for its diagonalized form).  Everything
-per step runs on the device (``rk_dense_evolve``): the FP64 psi-matrices whenever h changes,
-the stages as 3xTF32 tcgen05 GEMMs with FP32 accumulation, the error test and the
-accept/reject rule.  The batch steps in lockstep with one h (an attempt is accepted when
-every instance passes; a one-instance batch follows the reference's controller exactly).
+spectrum; rkstiff/etd35.py:412-420 does the same for its diagonalized form).  Two device
+paths, both whole evolve loops on the GPU:
+
+* ``controller="instance"`` (default, ``rk_dense_eig_evolve``): every instance under the
+  reference's accept/reject rule with its own h, as a loop of single-instance solvers would
+  run; stages in the eigenbasis with per-instance diagonal coefficients, the basis changes
+  S k and S^-1 N as 3xTF32 tcgen05 GEMMs, one persistent launch;
+* ``controller="lockstep"`` (``rk_dense_evolve``): one h for the batch (an attempt is
+  accepted when every instance passes), FP64 psi-matrices rebuilt when h changes, one
+  K-concatenated 3xTF32 GEMM per stage.
+
+A one-instance batch follows the reference's controller on either path.
 """
 
 from __future__ import annotations
@@ -29,7 +36,7 @@ class DenseEnsemble:
 
     def __init__(self, lin_op, nl_func: BuiltinNL, n_inst: int, config: Optional[SolverConfig] = None,
                  etd_config: Optional[ETDConfig] = None, device=None, method: str = "ETD35",
-                 err_basis: str = "physical", controller: str = "lockstep"):
+                 err_basis: str = "physical", controller: str = "instance"):
         """``err_basis``: "physical" forms the embedded error vector in physical space, as the
         reference's non-diagonal ETD35 does (etd35.py:719); "eigen" forms it in the eigenbasis
         (S^-1 applied) with the mask taken from the physical state, as the reference's
@@ -200,7 +207,7 @@ def _main(argv=None) -> None:
     ap.add_argument("--tf", type=float, default=70.0)
     ap.add_argument("--epsilon", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=5)
-    ap.add_argument("--controller", choices=["lockstep", "instance"], default="lockstep")
+    ap.add_argument("--controller", choices=["lockstep", "instance"], default="instance")
     args = ap.parse_args(argv)
     lin, nl, w0 = workloads.allen_cahn_batch(args.instances, args.seed)
     ens = DenseEnsemble(lin, nl, args.instances, config=SolverConfig(epsilon=args.epsilon),

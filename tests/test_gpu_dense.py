@@ -74,7 +74,7 @@ def test_one_attempt_matches_oracle():
     rng = np.random.default_rng(3)
     w0 = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi) - xi + 0.05 * rng.standard_normal(xi.size)
     h = 0.05
-    ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-3))
+    ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-3), controller="lockstep")
     u = ens.pack_u(w0[None, :])
     ens.put_state(ens.fresh_state(0.0, 10.0, h))
     st = ens.run(u, 1)
@@ -104,7 +104,7 @@ def test_allen_cahn_n20_matches_pinned_oracle(golden):
     w0 = g["ac20_w0"]
     errs = {}
     for tf in (10.0, 30.0):
-        ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4))
+        ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4), controller="lockstep")
         out = ens.evolve(w0[None, :], 0.0, tf).cpu().numpy()[0].astype(np.float64)
         st = ens.stats()
         s = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), dense_psi="eig")
@@ -121,9 +121,9 @@ def test_lockstep_batch_equals_single_instance():
     x, (lin, nl) = ac_ops(64)
     xi = x[1:-1]
     w0 = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi) - xi
-    one = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4))
+    one = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4), controller="lockstep")
     u1 = one.evolve(w0[None, :], 0.0, 5.0).cpu().numpy()
-    many = DenseEnsemble(lin, nl, 130, config=SolverConfig(epsilon=1e-4))  # three tiles, the last padded
+    many = DenseEnsemble(lin, nl, 130, config=SolverConfig(epsilon=1e-4), controller="lockstep")  # three tiles, the last padded
     u2 = many.evolve(np.repeat(w0[None, :], 130, axis=0), 0.0, 5.0).cpu().numpy()
     np.testing.assert_array_equal(u2, np.repeat(u1, 130, axis=0))
     assert one.stats()["attempts"] == many.stats()["attempts"]
@@ -144,7 +144,7 @@ def test_config5_batch_against_tight_fp64():
     x, (lin, nl) = ac_ops(129)
     xi = x[1:-1]
     w0 = config5_ics(8192, 11, xi)
-    ens = DenseEnsemble(lin, nl, 8192, config=SolverConfig(epsilon=1e-4))
+    ens = DenseEnsemble(lin, nl, 8192, config=SolverConfig(epsilon=1e-4), controller="lockstep")
     out = ens.evolve(w0, 0.0, 70.0).cpu().numpy().astype(np.float64)
     st = ens.stats()
     assert st["status"] == nat.RK_ST_DONE and np.all(np.isfinite(out))
@@ -189,7 +189,7 @@ def test_diagonalized_error_semantics():
     x, (lin, nl) = ac_ops(20)
     xi = x[1:-1]
     w0 = 0.53 * xi + 0.47 * np.sin(-1.5 * np.pi * xi) - xi
-    ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4), err_basis="eigen")
+    ens = DenseEnsemble(lin, nl, 1, config=SolverConfig(epsilon=1e-4), err_basis="eigen", controller="lockstep")
     u = ens.pack_u(w0[None, :])
     ens.put_state(ens.fresh_state(0.0, 10.0, 0.05))
     st = ens.run(u, 1)
