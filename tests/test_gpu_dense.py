@@ -157,10 +157,14 @@ def test_config5_batch_against_tight_fp64():
 
 
 def test_solver_api_with_a_dense_operator():
-    """ETD35(lin_op_2d, Allen-Cahn, precision fp32) runs the tensor-core path with the reference's snapshot
-    semantics: a snapshot every store_freq accepted steps.  The error estimate cancels to
-    ~1e-5 of the stage values, so FP32 stages move s (and the next h) by ~1e-3 relative:
-    snapshot times agree to 5e-3, the final state at tf to 1e-4."""
+    """ETD35(lin_op_2d, Allen-Cahn, precision fp32) runs the tensor-core path with the
+    reference's snapshot semantics (solveras.py:622-646): t0, then a snapshot after every
+    store_freq-th accepted step.  The step sequence itself is not compared with the FP64
+    oracle: where the embedded error is near FP32 resolution (the first attempt here: s =
+    3.91 in FP64, err ~2e-7 |u|) FP32 stages move s by a few percent, so h and the snapshot
+    times drift from the FP64 ones (by up to ~10% here) while the states stay on the same
+    solution: each snapshot matches an FP64 oracle run to the snapshot's own time to 1e-3,
+    the final state at tf to 1e-4."""
     from rkstiff_gb300 import ETD35
 
     x, (lin, nl) = ac_ops(20)
@@ -169,13 +173,16 @@ def test_solver_api_with_a_dense_operator():
     solver = ETD35(lin_op=lin, nl_func=nl, config=SolverConfig(epsilon=1e-4), device_options=DeviceOptions(precision="fp32"))
     uf = solver.evolve(w0, t0=0.0, tf=5.0, store_freq=3)
     assert type(solver._engine()).__name__ == "DenseBackend"
-    ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-4), dense_psi="eig")
-    rf = ref.evolve(w0.astype(np.complex128), 0.0, 5.0, store_data=True, store_freq=3)
-    assert len(solver.t) == len(ref.t) and solver.t[-1] == 5.0
-    np.testing.assert_allclose(solver.t, ref.t, rtol=5e-3)
-    for a, b in zip(solver.u[1:], ref.u[1:]):
-        assert np.linalg.norm(np.asarray(a).real - b.real) <= 5e-3 * np.linalg.norm(b.real)
-    assert np.linalg.norm(np.asarray(uf).real - rf.real) <= 1e-4 * np.linalg.norm(rf.real)
+    steps = solver.stats["steps"]
+    assert len(solver.t) == 1 + steps // 3 and solver.t[0] == 0.0
+    assert np.all(np.diff(solver.t) > 0) and solver.t[-1] <= 5.0
+    for ti, ui in zip(solver.t[1:], solver.u[1:]):
+        ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-8), dense_psi="eig")
+        r = ref.evolve(w0.astype(np.complex128), 0.0, float(ti), store_data=False).real
+        assert np.linalg.norm(np.asarray(ui).real - r) <= 2e-5 * np.linalg.norm(r), ti
+    ref = O.OracleSolver("ETD35", lin, lambda v: nl(v), O.SolverConfig(epsilon=1e-8), dense_psi="eig")
+    rf = ref.evolve(w0.astype(np.complex128), 0.0, 5.0, store_data=False)
+    assert np.linalg.norm(np.asarray(uf).real - rf.real) <= 2e-5 * np.linalg.norm(rf.real)
     unew, h_used, h_next = solver.step(w0, 0.01)
     assert h_used == 0.01 and h_next > 0
 
