@@ -380,7 +380,8 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
   uint64_t* empty = full + NS;
   uint64_t* accb = empty + NS;  // chain c's accumulator complete (one phase per chain)
   uint64_t* epi = accb + 1;     // [2] epilogue c done (outputs written, slot c % 2 read): epi[c % 2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(epi + 2);
+  uint64_t* xb = epi + 2;       // exchanges among the epilogue threads (bounded, unlike bar.sync)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(xb + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, row = tid;
@@ -397,6 +398,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     tc::mbar_init(accb, 1);
     tc::mbar_init(&epi[0], 128);
     tc::mbar_init(&epi[1], 128);
+    tc::mbar_init(xb, 128);
     *abort_flag = 0;
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tmA);
@@ -487,6 +489,19 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
     // so no epilogue reads a stage vector back.
     const float xr = p.shift[row];
     float ev[NT], n2[NT], acc[32];
+    // all epilogue threads meet; a thread that gave up on an earlier wait never arrives, so
+    // the others time out here instead of waiting forever
+    int xphase = 0;
+    auto sync_epi = [&]() -> bool {
+      tc::mbar_arrive(xb);
+      const bool w = tc::mbar_wait(xb, (uint32_t)xphase & 1u, WAIT_NS);
+      ++xphase;
+      if (!w) {
+        atomicOr(&st->error, 2);
+        *abort_flag = 1;
+      }
+      return w;
+    };
 #pragma unroll 16
     for (int j = 0; j < NT; ++j) ev[j] = -vget(p, vN1, col0 + j, row);
     for (int c = 0; c < 6; ++c) {
@@ -550,7 +565,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
           }
         }
         tc::tc_fence_before();
-        tc::named_sync(1, 128);
+        if (!sync_epi()) break;
         const int j = tid >> 1, half = tid & 1;
         float mx = 0.f;
         int nan = 0;
@@ -598,7 +613,7 @@ __global__ void __launch_bounds__(ATTEMPT_THREADS, 1)
           cm[warp] = smin;
           cn[warp] = snan;
         }
-        tc::named_sync(1, 128);
+        if (!sync_epi()) break;
         if (tid == 0) {
           for (int i = 1; i < 4; ++i) {
             smin = fmin(smin, cm[i]);
