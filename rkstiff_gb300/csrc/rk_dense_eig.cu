@@ -27,6 +27,7 @@
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "rk_evolve.cuh"
 #include "rk_launch.h"
@@ -506,28 +507,30 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
         }
       }
       publish();
-      // stages 2..6: S k -> N in physical space -> S^-1 N = N_st; the next combination
-      for (int st = 2; st <= 6 && ok; ++st) {
-        if (!(ok = wait_acc())) break;
+      // stages 2..6: S k -> N in physical space -> S^-1 N = N_st; the next combination.  One
+      // instantiation per stage, so that each keeps only the vectors it reads live.
+      auto stage = [&](auto stc) -> bool {
+        constexpr int st = decltype(stc)::value;
+        if (!wait_acc()) return false;
         load_acc();
 #pragma unroll
         for (int jj = 0; jj < 32; ++jj) dep_put(dep, row, j0 + jj, nl_ac(acc[jj], xr));
         publish();
-        if (!(ok = wait_acc())) break;
+        if (!wait_acc()) return false;
 #pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           float nk[16], v[16], n1[16], x1[16], x2[16], x3[16];
           tld(T_ACC, sub, nk);
           tld(T_V, sub, v);
           tld(T_N1, sub, n1);
-          if (st == 4) {
+          if constexpr (st == 4) {
             tld(T_N2, sub, x1);
             tld(T_N3, sub, x2);
-          } else if (st == 5) {
+          } else if constexpr (st == 5) {
             tld(T_N2, sub, x1);
             tld(T_N3, sub, x2);
             tld(T_N4, sub, x3);
-          } else if (st == 6) {
+          } else if constexpr (st == 6) {
             tld(T_N3, sub, x1);
             tld(T_N4, sub, x2);
             tld(T_N5, sub, x3);
@@ -537,15 +540,15 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
           for (int k = 0; k < 16; ++k) {
             const int j = j0 + sub * 16 + k;
             // etd35.py:322-345
-            if (st == 2) {
+            if constexpr (st == 2) {
               dep_put(dep, row, j, (cf(j, C35_E14) * v[k] + cf(j, C35_A31) * n1[k]) + cf(j, C35_A32) * nk[k]);
-            } else if (st == 3) {
+            } else if constexpr (st == 3) {
               dep_put(dep, row, j, (cf(j, C35_E12) * v[k] + cf(j, C35_A41) * n1[k]) + cf(j, C35_A43) * nk[k]);
-            } else if (st == 4) {
+            } else if constexpr (st == 4) {
               dep_put(dep, row, j,
                       ((cf(j, C35_E34) * v[k] + cf(j, C35_A51) * n1[k]) + cf(j, C35_A52) * (x1[k] - x2[k])) +
                           cf(j, C35_A54) * nk[k]);
-            } else if (st == 5) {
+            } else if constexpr (st == 5) {
               const float t = x1[k] - (3.f * x3[k]) * 0.5f;
               dep_put(dep, row, j,
                       (((cf(j, C35_E) * v[k] + cf(j, C35_A61) * n1[k]) + cf(j, C35_A62) * t) + cf(j, C35_A63) * x2[k]) +
@@ -563,8 +566,12 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
           tst(st < 6 ? T_N2 + st - 2 : T_UN, sub, nk);
         }
         tc::tmem_st_wait();
-        if (st < 6) publish();
-      }
+        if constexpr (st < 6) publish();
+        return true;
+      };
+      ok = stage(std::integral_constant<int, 2>{}) && stage(std::integral_constant<int, 3>{}) &&
+           stage(std::integral_constant<int, 4>{}) && stage(std::integral_constant<int, 5>{}) &&
+           stage(std::integral_constant<int, 6>{});
       if (!ok) break;
       if (!p.err_eigen) {
         // S err: the error vector in physical space (etd35.py:719)
