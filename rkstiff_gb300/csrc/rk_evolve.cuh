@@ -121,7 +121,9 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
   const Group& g = x.g;
   // FFT-buffer index: padded for the compile-time transforms
   auto P = [](int c) { return LOGN > 0 ? fpad(c) : c; };
-  if (x.nl_kind == RK_NL_UUX) {
+  // the compile-time-size kernels serve u*ux only (rk_m_etd35_ct.cu dispatches nothing else
+  // to them), so they carry no other nonlinearity's code
+  if (LOGN > 0 || x.nl_kind == RK_NL_UUX) {
     // u = irfft(k), ux = irfft(i kx k) packed as one complex inverse FFT of length n:
     // Z = A + iB with A, B the Hermitian spectra; numpy's irfft drops the imaginary
     // parts of the DC and Nyquist bins, so they are dropped here too.
@@ -195,6 +197,8 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
       }
     }
     g.sync();
+  } else if constexpr (LOGN > 0) {
+    // not reached
   } else if (x.nl_kind == RK_NL_NLS) {
     // v = ifft(k); N = fft(i c |v|^2 v)
     const int n = LOGN > 0 ? (1 << LOGN) : x.n;

@@ -1,4 +1,5 @@
-// Dispatch to the compile-time-size ETD35 kernels (real operator, n = 256..2048).
+// Dispatch to the compile-time-size ETD35 kernels (real operator, the u*ux nonlinearity,
+// n = 256..2048).
 #include "rk_launch.h"
 
 namespace rk {
@@ -9,7 +10,7 @@ int launch_evolve_etd35_n1024(const rk_batch& b, const ClassLaunch& c, cudaStrea
 int launch_evolve_etd35_n2048(const rk_batch& b, const ClassLaunch& c, cudaStream_t s);
 
 int launch_evolve_etd35_ct(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
-  if (b.coef_complex || c.n <= 0 || b.nl_kind == RK_NL_NONE) return RK_E_UNSUPPORTED;
+  if (b.coef_complex || c.n <= 0 || b.nl_kind != RK_NL_UUX) return RK_E_UNSUPPORTED;
   switch (c.n) {
     case 256: return launch_evolve_etd35_n256(b, c, s);
     case 512: return launch_evolve_etd35_n512(b, c, s);
