@@ -108,16 +108,53 @@ RK_DEV dd dd_from_double(double v) {
   return dd{hi, (float)(v - (double)hi)};
 }
 
-// FP32 ETD coefficients of a real mode z = h lambda (|z| >= modecutoff, z <= 80) in
-// double-float arithmetic, h given as a double-float: method ETD35/ETD5 (21 values, layout
-// C35_*) or ETD34/ETD4 (10, C34_*).  The psi forms are those of fast_real_psi, reassociated
-// so that no intermediate leaves FP32 range for |z| up to ~1e18; the combinations follow
-// etd_from_psi_e.
-RK_DEV void dd_etd_coeffs(int method, double zd, dd h, float* o) {
+// s1 = (e^x - 1)/x, s2 = (e^x - 1 - x)/x^2, s3 = (e^x - 1 - x - x^2/2)/x^3 by their Taylor
+// series (sum x^k / (k + j)!), 16 terms: below 2^-48 relative for |x| <= 1 (ETDConfig caps
+// modecutoff at 1).  The inverse factorials 1/(k+3)! as double-float pairs.
+RK_DEV void dd_taylor_s123(dd x, dd& s1, dd& s2, dd& s3) {
+  constexpr float F[16][2] = {{0x1.5555560000000p-3f, -0x1.5555560000000p-28f},
+                              {0x1.5555560000000p-5f, -0x1.5555560000000p-30f},
+                              {0x1.1111120000000p-7f, -0x1.ddddde0000000p-32f},
+                              {0x1.6c16c20000000p-10f, -0x1.27d27e0000000p-35f},
+                              {0x1.a01a020000000p-13f, -0x1.7f97fa0000000p-39f},
+                              {0x1.a01a020000000p-16f, -0x1.7f97fa0000000p-42f},
+                              {0x1.71de3a0000000p-19f, 0x1.55b1cc0000000p-45f},
+                              {0x1.27e4fc0000000p-22f, -0x1.10ec140000000p-47f},
+                              {0x1.ae64560000000p-26f, 0x1.fd51380000000p-52f},
+                              {0x1.1eed8e0000000p-29f, 0x1.ff1b140000000p-54f},
+                              {0x1.6124620000000p-33f, -0x1.8af25e0000000p-58f},
+                              {0x1.93974a0000000p-37f, 0x1.180f940000000p-62f},
+                              {0x1.ae7f3e0000000p-41f, 0x1.ccee080000000p-67f},
+                              {0x1.ae7f3e0000000p-45f, 0x1.ccee080000000p-71f},
+                              {0x1.952c780000000p-49f, -0x1.f9ea560000000p-74f},
+                              {0x1.6827860000000p-53f, 0x1.dcbecc0000000p-80f}};
+  dd acc{F[15][0], F[15][1]};
+#pragma unroll
+  for (int k = 14; k >= 0; --k) acc = dd{F[k][0], F[k][1]} + x * acc;
+  s3 = acc;
+  s2 = dd_of(0.5f) + x * s3;
+  s1 = dd_of(1.f) + x * s2;
+}
+
+// FP32 ETD coefficients of a real mode z = h lambda (z <= 80) in double-float arithmetic,
+// h given as a double-float: method ETD35/ETD5 (21 values, layout C35_*) or ETD34/ETD4 (10,
+// C34_*).  For |z| >= modecutoff the psi forms are those of fast_real_psi, reassociated so
+// that no intermediate leaves FP32 range for |z| up to ~1e18; below it (`small`) the
+// psi functions come from their Taylor series, as the FP64 build does.  The combinations
+// follow etd_from_psi_e.
+RK_DEV void dd_etd_coeffs(int method, double zd, dd h, float* o, bool small = false) {
   const dd z = dd_from_double(zd);
-  const dd rz = dd_recip(z);
-  // h psi_1..3 of x = c z from e^x - 1 and r = 1/x
+  const dd rz = small ? dd_of(0.f) : dd_recip(z);
+  // h psi_1..3 of x = c z from e^x - 1 and r = 1/x (or the series)
   auto psis = [&](dd x, dd em1, dd r, dd* P, bool third) {
+    if (small) {
+      dd s1, s2, s3;
+      dd_taylor_s123(x, s1, s2, s3);
+      P[0] = h * s1;
+      P[1] = scale2(h, 2.f) * s2;
+      if (third) P[2] = (h * 6.f) * s3;
+      return;
+    }
     const dd d = em1 - x;
     const dd dr = d * r;
     P[0] = h * (em1 * r);

@@ -105,18 +105,12 @@ RK_DEV float nl_ac(float w, float x) {
   return x - v * v * v;
 }
 
-// FP32 ETD35 coefficients of one real mode z = h lambda (layout C35_*): the Taylor series
-// below modecutoff, double-float arithmetic up to z = 80, FP64 beyond; the branches of the
-// diagonal path's FP32 coefficient build.
+// FP32 ETD35 coefficients of one real mode z = h lambda (layout C35_*): double-float
+// arithmetic up to z = 80 (the Taylor series below modecutoff), FP64 beyond; the branches of
+// the diagonal path's FP32 coefficient build.
 RK_DEV void etd35_mode_f32(double z, double h, const EtdCfg& ec, float* out) {
-  if (fabs(z) < ec.cutoff) {
-    double E[4], P[RK_PSI35_N], o[C35_N];
-    taylor_psi<double>(RK_ETD35, z, h, E, P);
-    etd_from_psi_e<double>(RK_ETD35, E, P, o);
-#pragma unroll
-    for (int c = 0; c < C35_N; ++c) out[c] = (float)o[c];
-  } else if (z <= 80.0) {
-    dd_etd_coeffs(RK_ETD35, z, dd_from_double(h), out);
+  if (z <= 80.0) {
+    dd_etd_coeffs(RK_ETD35, z, dd_from_double(h), out, fabs(z) < ec.cutoff);
   } else {
     double E[4], P[RK_PSI35_N], o[C35_N];
     fast_real_psi(RK_ETD35, z, h, E, P);

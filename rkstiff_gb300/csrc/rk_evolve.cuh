@@ -285,11 +285,20 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     S o[NC];
     if constexpr (FAST) {
       if (small) {
-        S E[4];
-        taylor_psi<S>(METHOD, z, h, E, P);
-        etd_from_psi_e<S>(METHOD, E, P, o);
+        if constexpr (sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float)) {
+          // the series in double-float on the FP32 pipes: the FP64 series would hold the
+          // whole warp on the 1/64-rate FP64 pipe for one small mode
+          float of[NC];
+          dd_etd_coeffs(METHOD, sre(z), hdd, of, true);
 #pragma unroll
-        for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+          for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+        } else {
+          S E[4];
+          taylor_psi<S>(METHOD, z, h, E, P);
+          etd_from_psi_e<S>(METHOD, E, P, o);
+#pragma unroll
+          for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+        }
         continue;
       }
     }

@@ -115,3 +115,28 @@ def test_config5_sample_against_tight_fp64():
         err = np.linalg.norm(out[i] - ref) / np.linalg.norm(ref)
         print(f"config-5 instance {i}: rel L2 vs FP64 eps=1e-8 {err:.3e} (attempts {st['attempts'][i]})")
         assert err <= 2e-3, (i, err)
+
+
+def test_calls_continue_bitwise():
+    """A run split into calls of a few attempts each (the state and N1 carried in the work
+    buffer between calls) gives bitwise the run of one call."""
+    x, (lin, nl) = ac_ops(64)
+    xi = x[1:-1]
+    w0 = ics(70, 2, xi)
+    one = DenseEnsemble(lin, nl, 70, config=SolverConfig(epsilon=1e-4), controller="instance")
+    u1 = one.evolve(w0, 0.0, 3.0).cpu().numpy()
+    s1 = one.stats()
+    split = DenseEnsemble(lin, nl, 70, config=SolverConfig(epsilon=1e-4), controller="instance")
+    u = split.pack_u(w0)
+    split.put_state(split.fresh_state(0.0, 3.0, 0.03))
+    calls = 0
+    while True:
+        st = split.run(u, 7)
+        calls += 1
+        if not np.any(st["status"] == nat.RK_ST_RUNNING):
+            break
+        assert calls < 1000
+    assert calls > 3
+    np.testing.assert_array_equal(u.cpu().numpy(), u1)
+    for k in ("steps", "attempts", "rejects", "nl_evals", "coeff_updates"):
+        np.testing.assert_array_equal(st[k], s1[k])
