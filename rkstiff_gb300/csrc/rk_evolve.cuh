@@ -81,9 +81,16 @@ struct Ctx {
 //
 // u*ux on a real grid: inverse FFT of n points, the product written as reals by the last
 // inverse pass, forward FFT of n/2 points, split into the n/2+1 rfft modes times c.
+// The FFT buffers and the twiddle table arrive as byte offsets into the kernel's dynamic
+// shared memory and are rebuilt from it here, so that the compiler knows they address shared
+// memory inside this out-of-line function (pointer arguments would be generic).
 template <class T, int LOGN>
-__device__ __noinline__ void uux_core(Group g, cx<T>* fa, cx<T>* fb, const cx<T>* tws, T c,
+__device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off, uint32_t tws_off, T c,
                                       cx<T>* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  cx<T>* fa = reinterpret_cast<cx<T>*>(smem + fa_off);
+  cx<T>* fb = reinterpret_cast<cx<T>*>(smem + fb_off);
+  const cx<T>* tws = reinterpret_cast<const cx<T>*>(smem + tws_off);
   constexpr int n = 1 << LOGN, M = n >> 1;
   // last inverse pass writes the real product u*ux; the forward transform of length n/2
   // reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
@@ -159,7 +166,11 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     g.sync();
     cx<T>* F;
     if constexpr (LOGN > 0) {
-      uux_core<T, LOGN>(g, x.fa, x.fb, x.tws, x.nl_c, out);
+      extern __shared__ __align__(16) unsigned char smem[];
+      auto off = [](const void* q) {
+        return (uint32_t)(reinterpret_cast<const unsigned char*>(q) - smem);
+      };
+      uux_core<T, LOGN>(g, off(x.fa), off(x.fb), off(x.tws), x.nl_c, out);
       return;
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
