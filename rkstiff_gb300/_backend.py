@@ -84,32 +84,33 @@ class DiagBackend:
 
 class DenseBackend:
     """One-instance dense ensemble (rkstiff_gb300.dense, per-instance controller) behind a
-    solver object with a 2-D lin_op: ETD35 stepped in the eigenbasis with FP32 states and
-    3xTF32 tensor-core basis changes, under the reference's controller."""
+    solver object with a 2-D lin_op: ETD35, ETD34 or IF34 stepped in the eigenbasis with FP32
+    states and 3xTF32 tensor-core basis changes, under the reference's controller."""
 
     @staticmethod
     def takes(solver) -> bool:
-        """ETD35, FP32, the built-in Allen-Cahn nonlinearity, n <= 128."""
+        """ETD35, ETD34 or IF34, FP32, the built-in Allen-Cahn nonlinearity, n <= 128."""
         from .models import BuiltinNL
 
         nl = solver.nl_func
-        return (solver._method_name == "ETD35" and solver.device_options.precision == "fp32"
+        return (solver._method_name in ("ETD35", "ETD34", "IF34") and solver.device_options.precision == "fp32"
                 and isinstance(nl, BuiltinNL) and nl.kind == nat.RK_NL_ALLEN_CAHN
                 and tuple(solver.lin_op.shape)[0] <= nat.RK_DENSE_NMAX)
 
     def __init__(self, solver, method: str):
         from .dense import DenseEnsemble
 
-        if method != "ETD35":
-            raise NotImplementedError(f"{method}: the dense (2-D lin_op) path implements ETD35")
+        if method not in ("ETD35", "ETD34", "IF34"):
+            raise NotImplementedError(f"{method}: the dense (2-D lin_op) tensor-core path implements ETD35, ETD34, IF34")
         opts = solver.device_options
         self.solver = solver
         # diagonalize=True: the error vector in the eigenbasis, as the reference's
-        # diagonalized ETD35 forms it (etd35.py:495); otherwise in physical space (etd35.py:719)
+        # diagonalized forms return it (etd35.py:495, etd34.py:303, if34.py:195); otherwise in
+        # physical space (etd35.py:719, etd34.py:435, if34.py:253)
         basis = "eigen" if getattr(solver, "diagonalize", False) else "physical"
         self.ens = DenseEnsemble(solver.lin_op, solver.nl_func, 1, config=getattr(solver, "config", None),
                                  etd_config=getattr(solver, "etd_config", None), device=opts.device,
-                                 err_basis=basis)
+                                 err_basis=basis, method=method)
         self.reset()
 
     def reset(self):

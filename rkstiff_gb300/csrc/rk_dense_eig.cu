@@ -1,22 +1,26 @@
-// Dense (non-diagonal) operator path with a per-instance controller: ETD35 for a batch of
-// instances sharing one n x n lin_op = S diag(eig) S^-1 (n <= 128, real spectrum), every
-// instance with its own step size under the reference's accept/reject rule.
+// Dense (non-diagonal) operator path with a per-instance controller: ETD35, ETD34 or IF34
+// for a batch of instances sharing one n x n lin_op = S diag(eig) S^-1 (n <= 128, real
+// spectrum), every instance with its own step size under the reference's accept/reject rule.
 //
-// The stepping follows the reference's diagonalized strategy (rkstiff/etd35.py:348-495):
-// the state is kept in the eigenbasis, v = S^-1 u; the stage combinations are elementwise
-// with the diagonal ETD35 coefficients of h_i eig (h_i the instance's step size, rebuilt
-// when it changes); each nonlinear evaluation is S^-1 N(S k).  The two basis changes of a
-// stage are 3xTF32 tcgen05 GEMMs (M = 128 vector rows, N = 64 instances per CTA, K = 128):
-// the coefficient operand (S or S^-1, TF32 hi/lo) streams through a TMA ring, the stage
-// operand is written by the previous epilogue straight into shared memory in the 128-byte
-// swizzled K-major tile layout.  One persistent CTA per 64 instances loops over attempts:
+// The stepping follows the reference's diagonalized strategy (rkstiff/etd35.py:348-495,
+// rkstiff/etd34.py:274-304, rkstiff/if34.py:164-196): the state is kept in the eigenbasis,
+// v = S^-1 u; the stage combinations are elementwise with the diagonal coefficients of
+// h_i eig (h_i the instance's step size, rebuilt when it changes); each nonlinear
+// evaluation is S^-1 N(S k).  The two basis changes of a stage are 3xTF32 tcgen05 GEMMs
+// (M = 128 vector rows, N = 64 instances per CTA, K = 128): the coefficient operand (S or
+// S^-1, TF32 hi/lo) streams through a TMA ring, the stage operand is written by the previous
+// epilogue straight into shared memory in the 128-byte swizzled K-major tile layout.  One
+// persistent CTA per 64 instances loops over attempts:
 //
-//   per attempt (13 GEMMs; 12 with the eigenbasis error vector):
+//   ETD35, per attempt (13 GEMMs; 12 with the eigenbasis error vector):
 //     k2 .. k6 (elementwise, eigenbasis) -> S k -> N (physical) -> S^-1 N -> N2 .. N6
 //     unew, err (elementwise) -> S err (physical error vector, etd35.py:719) ->
 //     S unew -> masked norms and s per instance (solveras.py:412-455) -> the reference's
 //     accept/reject rule per instance (solveras.py:457-554) -> S^-1 N(S unew) = N1 of the
 //     accepted state (ETD35 re-evaluates N(u) after an accepted step, etd35.py:310-318)
+//   ETD34 / IF34, per attempt (9 GEMMs; 8 with the eigenbasis error vector):
+//     k2 .. k4 -> N2 .. N4, unew -> S unew -> S^-1 N(S unew) = N5 -> err = c (N4 - N5) ->
+//     S err -> error test and rule; N1 = N5 of an accepted attempt (first same as last)
 //
 // Warps 0-7 are the epilogues (thread = vector row, 32 instances each), warp 8 issues the
 // MMAs, warp 9 the TMA loads.  Every wait is bounded by %globaltimer and reports through
@@ -105,19 +109,37 @@ RK_DEV float nl_ac(float w, float x) {
   return x - v * v * v;
 }
 
-// FP32 ETD35 coefficients of one real mode z = h lambda (layout C35_*): double-float
-// arithmetic up to z = 80 (the Taylor series below modecutoff), FP64 beyond; the branches of
-// the diagonal path's FP32 coefficient build.
-RK_DEV void etd35_mode_f32(double z, double h, const EtdCfg& ec, float* out) {
-  if (z <= 80.0) {
-    dd_etd_coeffs(RK_ETD35, z, dd_from_double(h), out, fabs(z) < ec.cutoff);
+// FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): double-float
+// arithmetic up to z = 80 (the psi Taylor series below modecutoff), FP64 beyond; the
+// branches of the diagonal path's FP32 coefficient build.
+template <int METHOD>
+RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
+  if constexpr (METHOD == RK_IF34) {
+    // e^z and e^(z/2) (if34.py:109-112)
+    if (z <= 80.0) {
+      dd m;
+      out[CIF_E] = dd_exp(dd_from_double(z), m).hi;
+      out[CIF_E2] = dd_exp(dd_from_double(0.5 * z), m).hi;
+    } else {
+      out[CIF_E] = (float)exp(z);
+      out[CIF_E2] = (float)exp(0.5 * z);
+    }
   } else {
-    double E[4], P[RK_PSI35_N], o[C35_N];
-    fast_real_psi(RK_ETD35, z, h, E, P);
-    etd_from_psi_e<double>(RK_ETD35, E, P, o);
+    constexpr int NP = METHOD == RK_ETD35 ? RK_PSI35_N : RK_PSI34_N;
+    constexpr int NC = METHOD == RK_ETD35 ? C35_N : C34_N;
+    if (z <= 80.0) {
+      dd_etd_coeffs(METHOD, z, dd_from_double(h), out, fabs(z) < ec.cutoff);
+    } else {
+      double E[4], P[NP], o[NC];
+      fast_real_psi(METHOD, z, h, E, P);
+      etd_from_psi_e<double>(METHOD, E, P, o);
 #pragma unroll
-    for (int c = 0; c < C35_N; ++c) out[c] = (float)o[c];
+      for (int c = 0; c < NC; ++c) out[c] = (float)o[c];
+    }
   }
+}
+template <int METHOD> __host__ __device__ constexpr int num_coeffs() {
+  return METHOD == RK_ETD35 ? C35_N : METHOD == RK_ETD34 ? C34_N : CIF_N;
 }
 
 // Element (instance j, K row `row`) of the stage operand in shared memory: the tile of the
@@ -198,19 +220,28 @@ __global__ void setup_kernel(float* A, double* eig_p, float* shift_p, int n, con
   }
 }
 
-// coefficient operand of GEMM q of an attempt of L GEMMs: the five stages alternate S (to
-// physical space) and S^-1 (back), then S err (physical error vector only), S unew, S^-1 N
+// Coefficient operand of GEMM q of an attempt of L GEMMs.  ETD35: the five stages
+// alternate S (to physical space) and S^-1 (back), then S err (physical error vector only),
+// S unew, S^-1 N(unew).  ETD34 / IF34: three stages and S unew -> S^-1 N(unew) alternate,
+// then S err (physical error vector only).
+template <int METHOD>
 RK_DEV int attempt_matrix(int q, int L) {
-  if (q < 10) return (q & 1) ? M_SI : M_S;
-  return q == L - 1 ? M_SI : M_S;
+  if constexpr (METHOD == RK_ETD35) {
+    if (q < 10) return (q & 1) ? M_SI : M_S;
+    return q == L - 1 ? M_SI : M_S;
+  } else {
+    return (q < 8 && (q & 1)) ? M_SI : M_S;
+  }
 }
 
 // the reference's accept/reject rule (solveras.py:457-554, the evolve loop's end-time
 // clamp, solveras.py:622-640) for one instance; returns 1 when the attempt is accepted
-RK_DEV int control_instance(rk_inst_state& s, double sv, const rk_controller& ctl) {
+// ETD35 evaluates N five times per attempt and N(unew) after an accepted one; the FSAL
+// methods (ETD34, IF34) four times per attempt, the last of them being N(unew).
+RK_DEV int control_instance(rk_inst_state& s, double sv, const rk_controller& ctl, bool fsal) {
   const double h = s.h;
   s.attempts += 1;
-  s.nl_evals += 5;
+  s.nl_evals += fsal ? 4 : 5;
   s.s_last = sv;
   if (isinf(sv) || isnan(sv) || sv < 1.0) {
     s.accept = 0;
@@ -222,7 +253,7 @@ RK_DEV int control_instance(rk_inst_state& s, double sv, const rk_controller& ct
     return 0;
   }
   s.accept = 1;
-  s.nl_evals += 1;  // N(unew), the next attempt's N1
+  if (!fsal) s.nl_evals += 1;  // N(unew), the next attempt's N1
   const double t = s.t + h;
   s.t = t;
   s.steps += 1;
@@ -244,6 +275,7 @@ RK_DEV int control_instance(rk_inst_state& s, double sv, const rk_controller& ct
 // Barrier phases: depr and accb complete once per GEMM (the stage operand of GEMM q is in
 // shared memory / GEMM q's accumulator is complete), go once per decision (decision 0 at the
 // start, decision a + 1 after attempt a's error test: continue or stop, in flags[0]).
+template <int METHOD>
 __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__ CUtensorMap tmA, Params p) {
   extern __shared__ unsigned char smem_raw[];
   // 1024-byte aligned by pointer arithmetic on the shared array (not through an integer),
@@ -267,7 +299,9 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t col0 = (int64_t)blockIdx.x * NT;
-  const int L = p.err_eigen ? 12 : 13;  // GEMMs per attempt
+  // GEMMs per attempt (one fewer with the eigenbasis error vector)
+  const int L = METHOD == RK_ETD35 ? (p.err_eigen ? 12 : 13) : (p.err_eigen ? 8 : 9);
+  constexpr int NCF = num_coeffs<METHOD>();
 
   if (tid == 0) {
     for (int i = 0; i < NS; ++i) {
@@ -312,7 +346,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     if (ok && !flags[0]) {
       if (p.first) ok = load_gemm(M_SI) && load_gemm(M_SI);
       for (int d = 1; ok; ++d) {
-        for (int q = 0; q < L && ok; ++q) ok = load_gemm(attempt_matrix(q, L));
+        for (int q = 0; q < L && ok; ++q) ok = load_gemm(attempt_matrix<METHOD>(q, L));
         if (ok) ok = tc::mbar_wait(go, (uint32_t)d & 1u, WAIT_NS);
         if (flags[0] || flags[1]) break;
       }
@@ -471,203 +505,365 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
       }
       tc::tmem_st_wait();
     }
+    // The error test of an attempt and the decision on the next (solveras.py:412-455 and
+    // 457-554 per instance): u2 holds |S unew|^2 per instance (NaN as +inf, which leaves
+    // every mask false and s NaN, as in the reference), acc the physical unew, e2 err^2.
+    // Max |u|^2 over the rows, then the sums of u^2 and err^2 over the rows with u^2 >
+    // cutoff^2 max |u|^2.  Rows: the 32 lanes of a warp (reduce-scatter: lane l ends with
+    // instance j0 + l) and the four lane quarters (shared memory).
+    auto error_test = [&](int a, bool& stop) -> bool {
+        warp_reduce_scatter32(u2, lane, [](float x, float y) { return fmaxf(x, y); });
+        red[(0 * 4 + quarter) * NT + j0 + lane] = u2[0];
+        if (!sync_epi()) return false;
+        const float cut2 = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff);
+  #pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int j = j0 + jj;
+          const float mx = fmaxf(fmaxf(red[j], red[NT + j]), fmaxf(red[2 * NT + j], red[3 * NT + j]));
+          const float up = acc[jj], a2 = up * up;
+          const bool m = a2 > cut2 * mx;
+          u2[jj] = m ? a2 : 0.f;
+          e2[jj] = m ? e2[jj] : 0.f;
+        }
+        warp_reduce_scatter32(u2, lane, [](float x, float y) { return x + y; });
+        warp_reduce_scatter32(e2, lane, [](float x, float y) { return x + y; });
+        red[(1 * 4 + quarter) * NT + j0 + lane] = u2[0];
+        red[(2 * 4 + quarter) * NT + j0 + lane] = e2[0];
+        if (!sync_epi()) return false;
+        if (tid < NT) {
+          acc_ok[tid] = 0;
+          if (own && so.status == RK_ST_RUNNING) {
+            double su = 0.0, se = 0.0;
+            for (int w = 0; w < 4; ++w) {
+              su += (double)red[(1 * 4 + w) * NT + tid];
+              se += (double)red[(2 * 4 + w) * NT + tid];
+            }
+            // s = safety (eps |u| / |err|)^(1/q), q = 4, as ratio^(1/8) of ratio = eps^2 su / se.
+            // An error vector that is exactly zero in FP32 while |u| > 0 (IF34's h (N4 - N5) / 6
+            // on a short last step) lies below FP32 resolution: the largest growth, MAX_S = 4,
+            // instead of the rejection x/0 = inf would give.
+            const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
+            const double sv = (se == 0.0 && su > 0.0 && !isinf(su)) ? 4.0
+                              : (ratio != ratio || isinf(ratio)) ? p.ctl.safety_f * ratio
+                                                                 : p.ctl.safety_f * pow(ratio, 0.125);
+            acc_ok[tid] = control_instance(so, sv, p.ctl, METHOD != RK_ETD35);
+          }
+        }
+        publish_state();
+        if (!sync_epi()) return false;
+        if (tid == 0) {
+          int any = 0;
+          for (int j = 0; j < NT; ++j) any |= running[j];
+          flags[0] = (!any || a + 1 >= p.max_attempts) ? 1 : 0;
+        }
+        if (!sync_epi()) return false;
+        stop = flags[0] != 0;
+        tc::mbar_arrive(go);
+      return true;
+    };
     for (int a = 0; ok && !stop0; ++a) {
       // coefficients of the instances whose h changed (this thread's mode and instances)
       for (int jj = 0; jj < 32; ++jj) {
         const int j = j0 + jj;
         if (!need[j]) continue;
-        float c[C35_N];
+        float c[NCF];
         const double h = hsm[j];
-        etd35_mode_f32(h * lam, h, p.ec, c);
+        mode_coeffs_f32<METHOD>(h * lam, h, p.ec, c);
         float* cp = p.C + ((col0 + j) * C35_N) * DM + row;
 #pragma unroll
-        for (int k = 0; k < C35_N; ++k) cp[k * DM] = c[k];
+        for (int k = 0; k < NCF; ++k) cp[k * DM] = c[k];
       }
       if (own && need[tid]) {
         so.h_coeff = so.h;
         so.coeff_updates += 1;
       }
-      // k2 = E14 v + a21 N1 (etd35.py:320)
-#pragma unroll
-      for (int sub = 0; sub < 2; ++sub) {
-        float v[16], n1[16];
-        tld(T_V, sub, v);
-        tld(T_N1, sub, n1);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const int j = j0 + sub * 16 + k;
-          dep_put(dep, row, j, cf(j, C35_E14) * v[k] + cf(j, C35_A21) * n1[k]);
-        }
-      }
-      publish();
-      // stages 2..6: S k -> N in physical space -> S^-1 N = N_st; the next combination.  One
-      // instantiation per stage, so that each keeps only the vectors it reads live.
-      auto stage = [&](auto stc) -> bool {
-        constexpr int st = decltype(stc)::value;
-        if (!wait_acc()) return false;
-        load_acc();
-#pragma unroll
-        for (int jj = 0; jj < 32; ++jj) dep_put(dep, row, j0 + jj, nl_ac(acc[jj], xr));
-        publish();
-        if (!wait_acc()) return false;
-#pragma unroll
+      bool stop = false;
+      if constexpr (METHOD == RK_ETD35) {
+        // k2 = E14 v + a21 N1 (etd35.py:320)
+  #pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
-          float nk[16], v[16], n1[16], x1[16], x2[16], x3[16];
-          tld(T_ACC, sub, nk);
+          float v[16], n1[16];
           tld(T_V, sub, v);
           tld(T_N1, sub, n1);
-          if constexpr (st == 4) {
-            tld(T_N2, sub, x1);
-            tld(T_N3, sub, x2);
-          } else if constexpr (st == 5) {
-            tld(T_N2, sub, x1);
-            tld(T_N3, sub, x2);
-            tld(T_N4, sub, x3);
-          } else if constexpr (st == 6) {
-            tld(T_N3, sub, x1);
-            tld(T_N4, sub, x2);
-            tld(T_N5, sub, x3);
+          tc::tmem_ld_wait();
+  #pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int j = j0 + sub * 16 + k;
+            dep_put(dep, row, j, cf(j, C35_E14) * v[k] + cf(j, C35_A21) * n1[k]);
           }
+        }
+        publish();
+        // stages 2..6: S k -> N in physical space -> S^-1 N = N_st; the next combination.  One
+        // instantiation per stage, so that each keeps only the vectors it reads live.
+        auto stage = [&](auto stc) -> bool {
+          constexpr int st = decltype(stc)::value;
+          if (!wait_acc()) return false;
+          load_acc();
+  #pragma unroll
+          for (int jj = 0; jj < 32; ++jj) dep_put(dep, row, j0 + jj, nl_ac(acc[jj], xr));
+          publish();
+          if (!wait_acc()) return false;
+  #pragma unroll
+          for (int sub = 0; sub < 2; ++sub) {
+            float nk[16], v[16], n1[16], x1[16], x2[16], x3[16];
+            tld(T_ACC, sub, nk);
+            tld(T_V, sub, v);
+            tld(T_N1, sub, n1);
+            if constexpr (st == 4) {
+              tld(T_N2, sub, x1);
+              tld(T_N3, sub, x2);
+            } else if constexpr (st == 5) {
+              tld(T_N2, sub, x1);
+              tld(T_N3, sub, x2);
+              tld(T_N4, sub, x3);
+            } else if constexpr (st == 6) {
+              tld(T_N3, sub, x1);
+              tld(T_N4, sub, x2);
+              tld(T_N5, sub, x3);
+            }
+            tc::tmem_ld_wait();
+  #pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              const int j = j0 + sub * 16 + k;
+              // etd35.py:322-345
+              if constexpr (st == 2) {
+                dep_put(dep, row, j, (cf(j, C35_E14) * v[k] + cf(j, C35_A31) * n1[k]) + cf(j, C35_A32) * nk[k]);
+              } else if constexpr (st == 3) {
+                dep_put(dep, row, j, (cf(j, C35_E12) * v[k] + cf(j, C35_A41) * n1[k]) + cf(j, C35_A43) * nk[k]);
+              } else if constexpr (st == 4) {
+                dep_put(dep, row, j,
+                        ((cf(j, C35_E34) * v[k] + cf(j, C35_A51) * n1[k]) + cf(j, C35_A52) * (x1[k] - x2[k])) +
+                            cf(j, C35_A54) * nk[k]);
+              } else if constexpr (st == 5) {
+                const float t = x1[k] - (3.f * x3[k]) * 0.5f;
+                dep_put(dep, row, j,
+                        (((cf(j, C35_E) * v[k] + cf(j, C35_A61) * n1[k]) + cf(j, C35_A62) * t) + cf(j, C35_A63) * x2[k]) +
+                            cf(j, C35_A65) * nk[k]);
+              } else {
+                const float un = ((((cf(j, C35_E) * v[k] + cf(j, C35_A71) * n1[k]) + cf(j, C35_A73) * x1[k]) +
+                                   cf(j, C35_A74) * x2[k]) + cf(j, C35_A75) * x3[k]) + cf(j, C35_A76) * nk[k];
+                const float er =
+                    cf(j, C35_A75) * ((((-n1[k] + 4.f * x1[k]) - 6.f * x2[k]) + 4.f * x3[k]) - nk[k]);
+                nk[k] = un;  // stored as unew below
+                if (p.err_eigen) e2[sub * 16 + k] = er * er;
+                else dep_put(dep, row, j, er);
+              }
+            }
+            tst(st < 6 ? T_N2 + st - 2 : T_UN, sub, nk);
+          }
+          tc::tmem_st_wait();
+          if constexpr (st < 6) publish();
+          return true;
+        };
+        ok = stage(std::integral_constant<int, 2>{}) && stage(std::integral_constant<int, 3>{}) &&
+             stage(std::integral_constant<int, 4>{}) && stage(std::integral_constant<int, 5>{}) &&
+             stage(std::integral_constant<int, 6>{});
+        if (!ok) break;
+        if (!p.err_eigen) {
+          // S err: the error vector in physical space (etd35.py:719)
+          publish();
+          if (!(ok = wait_acc())) break;
+          load_acc();
+  #pragma unroll
+          for (int jj = 0; jj < 32; ++jj) e2[jj] = acc[jj] * acc[jj];
+        }
+  #pragma unroll
+        for (int sub = 0; sub < 2; ++sub) {
+          float un[16];
+          tld(T_UN, sub, un);
+          tc::tmem_ld_wait();
+  #pragma unroll
+          for (int k = 0; k < 16; ++k) dep_put(dep, row, j0 + sub * 16 + k, un[k]);
+        }
+        publish();
+        if (!(ok = wait_acc())) break;
+        // S unew: the physical new state; N(S unew) for the next attempt's N1
+        load_acc();
+  #pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const float up = acc[jj];
+          const float a2 = up * up;
+          u2[jj] = a2 != a2 ? INFINITY : a2;
+          dep_put(dep, row, j0 + jj, nl_ac(up, xr));
+        }
+        publish();
+        if (!(ok = error_test(a, stop))) break;
+        // the physical new state is in acc until the next load; keep it in u2 for the update
+  #pragma unroll
+        for (int jj = 0; jj < 32; ++jj) u2[jj] = acc[jj];
+        if (!(ok = wait_acc())) break;
+        // accepted instances take the new state and N1 = S^-1 N(S unew)
+  #pragma unroll
+        for (int sub = 0; sub < 2; ++sub) {
+          float n1n[16], n1[16], v[16], un[16];
+          tld(T_ACC, sub, n1n);
+          tld(T_N1, sub, n1);
+          tld(T_V, sub, v);
+          tld(T_UN, sub, un);
+          tc::tmem_ld_wait();
+  #pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int j = j0 + sub * 16 + k;
+            if (acc_ok[j]) {
+              n1[k] = n1n[k];
+              v[k] = un[k];
+              V(V_UP, j) = u2[sub * 16 + k];
+            }
+          }
+          tst(T_N1, sub, n1);
+          tst(T_V, sub, v);
+        }
+        tc::tmem_st_wait();
+      } else {
+        // k2 (etd34.py:293, if34.py:185)
+#pragma unroll
+        for (int sub = 0; sub < 2; ++sub) {
+          float v[16], n1[16];
+          tld(T_V, sub, v);
+          tld(T_N1, sub, n1);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int k = 0; k < 16; ++k) {
             const int j = j0 + sub * 16 + k;
-            // etd35.py:322-345
-            if constexpr (st == 2) {
-              dep_put(dep, row, j, (cf(j, C35_E14) * v[k] + cf(j, C35_A31) * n1[k]) + cf(j, C35_A32) * nk[k]);
-            } else if constexpr (st == 3) {
-              dep_put(dep, row, j, (cf(j, C35_E12) * v[k] + cf(j, C35_A41) * n1[k]) + cf(j, C35_A43) * nk[k]);
-            } else if constexpr (st == 4) {
-              dep_put(dep, row, j,
-                      ((cf(j, C35_E34) * v[k] + cf(j, C35_A51) * n1[k]) + cf(j, C35_A52) * (x1[k] - x2[k])) +
-                          cf(j, C35_A54) * nk[k]);
-            } else if constexpr (st == 5) {
-              const float t = x1[k] - (3.f * x3[k]) * 0.5f;
-              dep_put(dep, row, j,
-                      (((cf(j, C35_E) * v[k] + cf(j, C35_A61) * n1[k]) + cf(j, C35_A62) * t) + cf(j, C35_A63) * x2[k]) +
-                          cf(j, C35_A65) * nk[k]);
+            if constexpr (METHOD == RK_ETD34) {
+              dep_put(dep, row, j, cf(j, C34_E2) * v[k] + cf(j, C34_A21) * n1[k]);
             } else {
-              const float un = ((((cf(j, C35_E) * v[k] + cf(j, C35_A71) * n1[k]) + cf(j, C35_A73) * x1[k]) +
-                                 cf(j, C35_A74) * x2[k]) + cf(j, C35_A75) * x3[k]) + cf(j, C35_A76) * nk[k];
-              const float er =
-                  cf(j, C35_A75) * ((((-n1[k] + 4.f * x1[k]) - 6.f * x2[k]) + 4.f * x3[k]) - nk[k]);
-              nk[k] = un;  // stored as unew below
-              if (p.err_eigen) e2[sub * 16 + k] = er * er;
-              else dep_put(dep, row, j, er);
+              const float e2c = cf(j, CIF_E2);
+              dep_put(dep, row, j, e2c * v[k] + (0.5f * (float)hsm[j]) * (e2c * n1[k]));
             }
           }
-          tst(st < 6 ? T_N2 + st - 2 : T_UN, sub, nk);
         }
-        tc::tmem_st_wait();
-        if constexpr (st < 6) publish();
-        return true;
-      };
-      ok = stage(std::integral_constant<int, 2>{}) && stage(std::integral_constant<int, 3>{}) &&
-           stage(std::integral_constant<int, 4>{}) && stage(std::integral_constant<int, 5>{}) &&
-           stage(std::integral_constant<int, 6>{});
-      if (!ok) break;
-      if (!p.err_eigen) {
-        // S err: the error vector in physical space (etd35.py:719)
         publish();
+        // stages 2..4: S k -> N in physical space -> S^-1 N = N_st; the next combination, the
+        // last of them unew (written as the operand of S unew).  One instantiation per stage.
+        auto stage = [&](auto stc) -> bool {
+          constexpr int st = decltype(stc)::value;
+          if (!wait_acc()) return false;
+          load_acc();
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) dep_put(dep, row, j0 + jj, nl_ac(acc[jj], xr));
+          publish();
+          if (!wait_acc()) return false;
+#pragma unroll
+          for (int sub = 0; sub < 2; ++sub) {
+            float nk[16], v[16], n1[16], x1[16], x2[16];
+            tld(T_ACC, sub, nk);
+            tld(T_V, sub, v);
+            if constexpr (METHOD == RK_ETD34 || st == 4) tld(T_N1, sub, n1);
+            if constexpr (st == 4) {
+              tld(T_N2, sub, x1);
+              tld(T_N3, sub, x2);
+            }
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              const int j = j0 + sub * 16 + k;
+              float kv;
+              if constexpr (METHOD == RK_ETD34) {
+                // etd34.py:295-301
+                if constexpr (st == 2) {
+                  kv = (cf(j, C34_E2) * v[k] + cf(j, C34_A31) * n1[k]) + cf(j, C34_A32) * nk[k];
+                } else if constexpr (st == 3) {
+                  kv = (cf(j, C34_E) * v[k] + cf(j, C34_A41) * n1[k]) + cf(j, C34_A43) * nk[k];
+                } else {
+                  kv = ((cf(j, C34_E) * v[k] + cf(j, C34_A51) * n1[k]) + cf(j, C34_A52) * (x1[k] + x2[k])) +
+                       cf(j, C34_A54) * nk[k];
+                }
+              } else {
+                // if34.py:186-193
+                const float h = (float)hsm[j];
+                if constexpr (st == 2) {
+                  kv = cf(j, CIF_E2) * v[k] + (0.5f * h) * nk[k];
+                } else if constexpr (st == 3) {
+                  kv = cf(j, CIF_E) * v[k] + h * (cf(j, CIF_E2) * nk[k]);
+                } else {
+                  const float e = cf(j, CIF_E), e2c = cf(j, CIF_E2);
+                  kv = e * v[k] + h * ((((e * n1[k]) * (1.f / 6.f) + (e2c * x1[k]) * (1.f / 3.f)) +
+                                        (e2c * x2[k]) * (1.f / 3.f)) + nk[k] * (1.f / 6.f));
+                }
+              }
+              dep_put(dep, row, j, kv);
+              if constexpr (st == 4) v[k] = kv;
+            }
+            tst(T_N2 + st - 2, sub, nk);
+            if constexpr (st == 4) tst(T_UN, sub, v);
+          }
+          tc::tmem_st_wait();
+          publish();
+          return true;
+        };
+        ok = stage(std::integral_constant<int, 2>{}) && stage(std::integral_constant<int, 3>{}) &&
+             stage(std::integral_constant<int, 4>{});
+        if (!ok) break;
+        // S unew: the physical new state (kept in the free slot T_N2 for the update) ->
+        // N(S unew) -> S^-1 N = N5, the next attempt's N1 when accepted
         if (!(ok = wait_acc())) break;
         load_acc();
+        tst(T_N2, 0, acc);
+        tst(T_N2, 1, acc + 16);
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) e2[jj] = acc[jj] * acc[jj];
-      }
-#pragma unroll
-      for (int sub = 0; sub < 2; ++sub) {
-        float un[16];
-        tld(T_UN, sub, un);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int k = 0; k < 16; ++k) dep_put(dep, row, j0 + sub * 16 + k, un[k]);
-      }
-      publish();
-      if (!(ok = wait_acc())) break;
-      // S unew: the physical new state; N(S unew) for the next attempt's N1
-      load_acc();
-#pragma unroll
-      for (int jj = 0; jj < 32; ++jj) {
-        const float up = acc[jj];
-        const float a2 = up * up;
-        u2[jj] = a2 != a2 ? INFINITY : a2;
-        dep_put(dep, row, j0 + jj, nl_ac(up, xr));
-      }
-      publish();
-      // error test per instance (solveras.py:412-455): max |u|^2 over the rows (NaN as +inf,
-      // which leaves every mask false and s NaN, as in the reference), then the sums of u^2
-      // and err^2 over the rows with u^2 > cutoff^2 max |u|^2.  Rows: the 32 lanes of a warp
-      // (reduce-scatter: lane l ends with instance j0 + l) and the four lane quarters (shared)
-      warp_reduce_scatter32(u2, lane, [](float x, float y) { return fmaxf(x, y); });
-      red[(0 * 4 + quarter) * NT + j0 + lane] = u2[0];
-      if (!(ok = sync_epi())) break;
-      const float cut2 = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff);
-#pragma unroll
-      for (int jj = 0; jj < 32; ++jj) {
-        const int j = j0 + jj;
-        const float mx = fmaxf(fmaxf(red[j], red[NT + j]), fmaxf(red[2 * NT + j], red[3 * NT + j]));
-        const float up = acc[jj], a2 = up * up;
-        const bool m = a2 > cut2 * mx;
-        u2[jj] = m ? a2 : 0.f;
-        e2[jj] = m ? e2[jj] : 0.f;
-      }
-      warp_reduce_scatter32(u2, lane, [](float x, float y) { return x + y; });
-      warp_reduce_scatter32(e2, lane, [](float x, float y) { return x + y; });
-      red[(1 * 4 + quarter) * NT + j0 + lane] = u2[0];
-      red[(2 * 4 + quarter) * NT + j0 + lane] = e2[0];
-      if (!(ok = sync_epi())) break;
-      if (tid < NT) {
-        acc_ok[tid] = 0;
-        if (own && so.status == RK_ST_RUNNING) {
-          double su = 0.0, se = 0.0;
-          for (int w = 0; w < 4; ++w) {
-            su += (double)red[(1 * 4 + w) * NT + tid];
-            se += (double)red[(2 * 4 + w) * NT + tid];
-          }
-          // s = safety (eps |u| / |err|)^(1/q), q = 4, as ratio^(1/8) of ratio = eps^2 su / se
-          const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
-          const double sv = (ratio != ratio || isinf(ratio)) ? p.ctl.safety_f * ratio
-                                                              : p.ctl.safety_f * pow(ratio, 0.125);
-          acc_ok[tid] = control_instance(so, sv, p.ctl);
+        for (int jj = 0; jj < 32; ++jj) {
+          const float up = acc[jj], a2 = up * up;
+          u2[jj] = a2 != a2 ? INFINITY : a2;
+          dep_put(dep, row, j0 + jj, nl_ac(up, xr));
         }
-      }
-      publish_state();
-      if (!(ok = sync_epi())) break;
-      if (tid == 0) {
-        int any = 0;
-        for (int j = 0; j < NT; ++j) any |= running[j];
-        flags[0] = (!any || a + 1 >= p.max_attempts) ? 1 : 0;
-      }
-      if (!(ok = sync_epi())) break;
-      const bool stop = flags[0] != 0;
-      tc::mbar_arrive(go);
-      // the physical new state is in acc until the next load; keep it in u2 for the update
+        tc::tmem_st_wait();
+        publish();
+        if (!(ok = wait_acc())) break;
+        // err = a54 (N4 - N5) (etd34.py:303) or h (N4 - N5) / 6 (if34.py:195)
 #pragma unroll
-      for (int jj = 0; jj < 32; ++jj) u2[jj] = acc[jj];
-      if (!(ok = wait_acc())) break;
-      // accepted instances take the new state and N1 = S^-1 N(S unew)
+        for (int sub = 0; sub < 2; ++sub) {
+          float n5[16], n4[16];
+          tld(T_ACC, sub, n5);
+          tld(T_N4, sub, n4);
+          tc::tmem_ld_wait();
 #pragma unroll
-      for (int sub = 0; sub < 2; ++sub) {
-        float n1n[16], n1[16], v[16], un[16];
-        tld(T_ACC, sub, n1n);
-        tld(T_N1, sub, n1);
-        tld(T_V, sub, v);
-        tld(T_UN, sub, un);
-        tc::tmem_ld_wait();
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const int j = j0 + sub * 16 + k;
-          if (acc_ok[j]) {
-            n1[k] = n1n[k];
-            v[k] = un[k];
-            V(V_UP, j) = u2[sub * 16 + k];
+          for (int k = 0; k < 16; ++k) {
+            const int j = j0 + sub * 16 + k;
+            const float c = METHOD == RK_ETD34 ? cf(j, C34_A54) : (float)hsm[j] * (1.f / 6.f);
+            const float er = c * (n4[k] - n5[k]);
+            if (p.err_eigen) e2[sub * 16 + k] = er * er;
+            else dep_put(dep, row, j, er);
           }
+          tst(T_N5, sub, n5);
         }
-        tst(T_N1, sub, n1);
-        tst(T_V, sub, v);
+        tc::tmem_st_wait();
+        if (!p.err_eigen) {
+          // S err: the error vector in physical space (the non-diagonal form's err)
+          publish();
+          if (!(ok = wait_acc())) break;
+          load_acc();
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) e2[jj] = acc[jj] * acc[jj];
+        }
+        // the physical new state back into acc for the error test
+        tld(T_N2, 0, acc);
+        tld(T_N2, 1, acc + 16);
+        tc::tmem_ld_wait();
+        if (!(ok = error_test(a, stop))) break;
+        // accepted instances take the new state and N1 = N5 (FSAL)
+#pragma unroll
+        for (int sub = 0; sub < 2; ++sub) {
+          float n5[16], n1[16], v[16], un[16];
+          tld(T_N5, sub, n5);
+          tld(T_N1, sub, n1);
+          tld(T_V, sub, v);
+          tld(T_UN, sub, un);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int j = j0 + sub * 16 + k;
+            if (acc_ok[j]) {
+              n1[k] = n5[k];
+              v[k] = un[k];
+              V(V_UP, j) = acc[sub * 16 + k];
+            }
+          }
+          tst(T_N1, sub, n1);
+          tst(T_V, sub, v);
+        }
+        tc::tmem_st_wait();
       }
-      tc::tmem_st_wait();
       if (stop) break;
     }
     if (!ok) flags[1] = 1;
@@ -710,11 +906,21 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
 // ---------------------------------------------------------------------------------
 // host
 // ---------------------------------------------------------------------------------
+template <int METHOD>
 int set_smem_attr() {
   static std::once_flag once;
   static cudaError_t e = cudaSuccess;
-  std::call_once(once, [] { e = cudaFuncSetAttribute(eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM); });
+  std::call_once(once,
+                 [] { e = cudaFuncSetAttribute(eig_kernel<METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM); });
   return cuda_check(e, "cudaFuncSetAttribute (dense eigenbasis kernel)");
+}
+
+template <int METHOD>
+int launch(const CUtensorMap& tmA, const Params& p, unsigned grid, cudaStream_t s) {
+  const int rc = set_smem_attr<METHOD>();
+  if (rc) return rc;
+  eig_kernel<METHOD><<<grid, THREADS, SMEM, s>>>(tmA, p);
+  return cuda_check(cudaGetLastError(), "rk_dense_eig_evolve launch");
 }
 
 }  // namespace dense_eig
@@ -733,8 +939,8 @@ extern "C" int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream) {
     set_error("rk_dense_eig_evolve: invalid batch");
     return RK_E_ARG;
   }
-  if (b->method != RK_ETD35 || b->nl_kind != RK_NL_ALLEN_CAHN) {
-    set_error("rk_dense_eig_evolve: the dense path implements ETD35 with the Allen-Cahn nonlinearity");
+  if ((b->method != RK_ETD35 && b->method != RK_ETD34 && b->method != RK_IF34) || b->nl_kind != RK_NL_ALLEN_CAHN) {
+    set_error("rk_dense_eig_evolve: the dense path implements ETD35, ETD34 and IF34 with the Allen-Cahn nonlinearity");
     return RK_E_UNSUPPORTED;
   }
   if (b->n < 1 || b->n > DM) {
@@ -749,8 +955,7 @@ extern "C" int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream) {
   const Layout L = layout(b->n_inst);
   unsigned char* w = static_cast<unsigned char*>(b->work);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  int rc = set_smem_attr();
-  if (rc) return rc;
+  int rc = RK_OK;
   Params p{};
   p.st = b->state;
   p.A = reinterpret_cast<const float*>(w + L.a);
@@ -778,8 +983,10 @@ extern "C" int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream) {
   CUtensorMap tmA;
   rc = make_tmap_f32_sw128(&tmA, p.A, DM, 2 * 2 * DM, DM);
   if (rc) return rc;
-  eig_kernel<<<(unsigned)(L.bpad / NT), THREADS, SMEM, s>>>(tmA, p);
-  rc = cuda_check(cudaGetLastError(), "rk_dense_eig_evolve launch");
+  const unsigned grid = (unsigned)(L.bpad / NT);
+  rc = b->method == RK_ETD35   ? launch<RK_ETD35>(tmA, p, grid, s)
+       : b->method == RK_ETD34 ? launch<RK_ETD34>(tmA, p, grid, s)
+                               : launch<RK_IF34>(tmA, p, grid, s);
   if (rc) return rc;
   return cuda_check(cudaStreamSynchronize(s), "rk_dense_eig_evolve");
 }

@@ -477,7 +477,11 @@ RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const 
     // (eps |u| / |err|)^(1/q) = ratio^(1/(2q)) with ratio = eps^2 su / se formed in FP64;
     // the fractional power runs in FP32 (FP64 pow is a long dependent chain on this GPU).
     // Edge values keep the reference's outcome: 0/0 -> NaN and x/0 -> inf (both rejected),
-    // a finite ratio beyond FP32 range stays finite (accepted).
+    // a finite ratio beyond FP32 range stays finite (accepted).  The one exception: an error
+    // vector that is exactly zero in FP32 while |u| > 0 lies below FP32 resolution (an FP64
+    // error of the same attempt is small but not zero), so the attempt takes the largest
+    // growth, MAX_S = 4, instead of the rejection that x/0 = inf would give.
+    if (se == 0.0 && su > 0.0 && !isinf(su)) return 4.0;
     double ratio = (ctl.epsilon * ctl.epsilon * su) / se;
     if (ratio != ratio || isinf(ratio)) return ctl.safety_f * ratio;
     float rf = (float)fmin(ratio, 1e30);

@@ -1,5 +1,6 @@
-"""Dense (non-diagonal) operators on the tensor cores: ETD35 for a batch of instances that
-share one n x n lin_op (n <= 128), e.g. the Allen-Cahn Chebyshev operator.
+"""Dense (non-diagonal) operators on the tensor cores: ETD35 (and, with the per-instance
+controller, ETD34 and IF34) for a batch of instances that share one n x n lin_op (n <= 128),
+e.g. the Allen-Cahn Chebyshev operator.
 
 The operator is diagonalised once on the host in FP64 (lin_op = S diag(eig) S^-1, real
 spectrum; rkstiff/etd35.py:412-420 does the same for its diagonalized form).  Two device
@@ -31,8 +32,8 @@ from .solveras import SolverConfig
 
 
 class DenseEnsemble:
-    """ETD35 with a dense ``lin_op`` for ``n_inst`` instances on one device (FP32 states,
-    FP64 coefficient matrices, 3xTF32 stage products)."""
+    """ETD35, ETD34 or IF34 with a dense ``lin_op`` for ``n_inst`` instances on one device
+    (FP32 states, FP64 operator factors, 3xTF32 stage products)."""
 
     def __init__(self, lin_op, nl_func: BuiltinNL, n_inst: int, config: Optional[SolverConfig] = None,
                  etd_config: Optional[ETDConfig] = None, device=None, method: str = "ETD35",
@@ -45,15 +46,21 @@ class DenseEnsemble:
         ``controller``: "lockstep" (one h for the batch, ``rk_dense_evolve``: psi-matrices and
         one K-concatenated GEMM per stage) or "instance" (every instance under the reference's
         controller with its own h, ``rk_dense_eig_evolve``: the stages in the eigenbasis with
-        per-instance diagonal coefficients, the basis changes as GEMMs)."""
+        per-instance diagonal coefficients, the basis changes as GEMMs).
+
+        ``method``: "ETD35" on either controller; "ETD34" and "IF34" (first same as last:
+        N1 of an accepted attempt is its N5) with the instance controller."""
         if err_basis not in ("physical", "eigen"):
             raise ValueError("err_basis must be 'physical' or 'eigen'")
         if controller not in ("lockstep", "instance"):
             raise ValueError("controller must be 'lockstep' or 'instance'")
         self.controller = controller
         self.err_eigen = 1 if err_basis == "eigen" else 0
-        if method != "ETD35":
-            raise NotImplementedError("the dense tensor-core path implements ETD35")
+        methods = ("ETD35", "ETD34", "IF34") if controller == "instance" else ("ETD35",)
+        if method not in methods:
+            raise NotImplementedError(f"the dense tensor-core path with the {controller} controller "
+                                      f"implements {', '.join(methods)}")
+        self.method = method
         if not isinstance(nl_func, BuiltinNL) or nl_func.kind != nat.RK_NL_ALLEN_CAHN:
             raise TypeError("the dense path runs the Allen-Cahn nonlinearity (rkstiff_gb300.models.allen_cahn_ops)")
         lin = np.asarray(lin_op)
@@ -137,7 +144,7 @@ class DenseEnsemble:
             raise ValueError("u must be a contiguous FP32 (n_inst, n) tensor on the ensemble's device")
         per_instance = self.controller == "instance"
         b = nat.RkDenseEigBatch() if per_instance else nat.RkDenseBatch()
-        b.method = nat.RK_ETD35
+        b.method = {"ETD35": nat.RK_ETD35, "ETD34": nat.RK_ETD34, "IF34": nat.RK_IF34}[self.method]
         b.n = self.n
         b.n_inst = self.n_inst
         b.nl_kind = nat.RK_NL_ALLEN_CAHN
@@ -208,10 +215,11 @@ def _main(argv=None) -> None:
     ap.add_argument("--epsilon", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--controller", choices=["lockstep", "instance"], default="instance")
+    ap.add_argument("--method", choices=["ETD35", "ETD34", "IF34"], default="ETD35")
     args = ap.parse_args(argv)
     lin, nl, w0 = workloads.allen_cahn_batch(args.instances, args.seed)
     ens = DenseEnsemble(lin, nl, args.instances, config=SolverConfig(epsilon=args.epsilon),
-                        controller=args.controller)
+                        controller=args.controller, method=args.method)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ens.evolve(w0, 0.0, args.tf)
