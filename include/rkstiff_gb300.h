@@ -325,15 +325,19 @@ int rk_dense_evolve(const rk_dense_batch* b, void* stream);
 /* Dense lin_op path with a per-instance controller: every instance follows the reference's
  * accept/reject rule with its own h (the rule of solveras.py:457-554 per instance, as a
  * loop of single-instance solvers would), stepped in the eigenbasis of lin_op = S diag(eig)
- * S^-1 as the reference's diagonalized ETD35 does (etd35.py:348-495): stage combinations
+ * S^-1 as the reference's diagonalized ETD35 / ETD34 / IF34 do (etd35.py:348-495,
+ * etd34.py:274-304, if34.py:164-196; ETD34 and IF34 carry N(unew) into the next attempt,
+ * first same as last): stage combinations
  * elementwise with per-instance diagonal coefficients (rebuilt for an instance when its h
  * changes), the basis changes S k and S^-1 N(S k) as 3xTF32 tensor-core GEMMs, one
  * persistent launch per call.  Same operator limits as rk_dense_evolve (real spectrum,
  * n <= RK_DENSE_NMAX, the Allen-Cahn nonlinearity).  The error vector is formed in
  * physical space (err_eigen = 0, the non-diagonal form etd35.py:719) or in the eigenbasis
- * (err_eigen = 1, etd35.py:495); the mask comes from the physical state either way. */
+ * (err_eigen = 1, etd35.py:495); the mask comes from the physical state either way.  An
+ * FP32 error vector that is exactly zero while |u| > 0 is accepted with s = 4 (below FP32
+ * resolution; the reference's x/0 = inf would reject it). */
 typedef struct rk_dense_eig_batch {
-  int32_t method;        /* RK_ETD35                                                      */
+  int32_t method;        /* RK_ETD35, RK_ETD34 or RK_IF34                                 */
   int32_t n;             /* vector length, 1..RK_DENSE_NMAX                               */
   int64_t n_inst;        /* instances                                                     */
   int32_t nl_kind;       /* RK_NL_ALLEN_CAHN                                              */
