@@ -349,6 +349,23 @@ def dense_measurement(dev) -> dict:
     lock = DenseEnsemble(lin, nl, DENSE["instances"], config=cfg, device=dev, controller="lockstep")
     lbest, _ = timed(lock)
     lst = lock.stats()
+    # the same kernel for the first-same-as-last methods (ETD34, IF34) on the same ICs, each
+    # checked on one IC against an FP64 oracle run at epsilon = 1e-8
+    methods = {}
+    for m in ("ETD34", "IF34"):
+        me = DenseEnsemble(lin, nl, DENSE["instances"], config=cfg, device=dev, method=m)
+        mbest, mout = timed(me)
+        mst = me.stats()
+        i0 = DENSE["reference_sample"][0]
+        o = O.OracleSolver(m, lin, lambda v: nl(v), O.SolverConfig(epsilon=DENSE["reference_epsilon"]),
+                           diagonalize=True)
+        ref = o.evolve(w0[i0].astype(np.complex128), 0.0, DENSE["tf"], store_data=False).real
+        mo = mout[i0].cpu().numpy().astype(np.float64)
+        methods[m] = {"seconds": mbest, "instances_per_s": DENSE["instances"] / mbest,
+                      "mode_steps_per_s": 128.0 * mst["steps_total"] / mbest,
+                      "attempts_total": mst["attempts_total"], "rejects_total": mst["rejects_total"],
+                      "all_done": bool(np.all(mst["status"] == 0)),
+                      f"rel_l2_vs_fp64_eps1e-8_ic{i0}": float(np.linalg.norm(mo - ref) / np.linalg.norm(ref))}
     out = out.cpu().numpy().astype(np.float64)
     errs = []
     for i in DENSE["reference_sample"]:
@@ -385,6 +402,7 @@ def dense_measurement(dev) -> dict:
                                   if "bf16_tflops" in peaks else "TF32 dense = half of the 1.9 PFLOP/s bf16 fallback",
                    "counted": "3 TF32 products x 13 basis changes (128 x 128 by the CTA's 64 instance vectors) "
                               "per instance-attempt; the stage combinations are elementwise, off the tensor pipe"},
+        "methods": methods,
         "lockstep": {"seconds": lbest, "instances_per_s": DENSE["instances"] / lbest,
                      "mode_steps_per_s": 128.0 * DENSE["instances"] * lst["steps"] / lbest,
                      "batch_attempts": lst["attempts"], "batch_steps": lst["steps"]},
