@@ -130,3 +130,26 @@ def test_grids_match_reference_golden(golden):
         rk.grids.construct_x_kx_rfft(7)
     x, kx = rk.grids.construct_x_kx_rfft(256, -30, 30)
     np.testing.assert_array_equal(kx, golden("fixed_step")["kdv_kx"])
+
+
+def test_dense_tensor_core_routing_and_methods():
+    """FP32 ETD35 / ETD34 / IF34 with a 2-D lin_op and the built-in Allen-Cahn nonlinearity
+    go to the tensor-core batch kernel (the per-instance controller); FP64, other methods
+    and other nonlinearities stay on the eigenbasis path.  The lockstep controller runs ETD35
+    only; methods outside the kernel are refused before any device work."""
+    from rkstiff_gb300 import DeviceOptions
+    from rkstiff_gb300._backend import DenseBackend
+    from rkstiff_gb300.dense import DenseEnsemble
+
+    x, D = P.cheb(20)
+    lin, nl = models.allen_cahn_ops(x, D, 0.01)
+    fp32 = DeviceOptions(precision="fp32")
+    for cls in (rk.ETD35, rk.ETD34, rk.IF34):
+        assert DenseBackend.takes(cls(lin, nl, device_options=fp32))
+        assert not DenseBackend.takes(cls(lin, nl))
+        assert not DenseBackend.takes(cls(lin, lambda u: u, device_options=fp32))
+    assert not DenseBackend.takes(rk.IF4(lin, nl, device_options=fp32))
+    for method, controller in (("IF34", "lockstep"), ("ETD34", "lockstep"), ("IF45DP", "instance"),
+                               ("ETD4", "instance")):
+        with pytest.raises(NotImplementedError):
+            DenseEnsemble(lin, nl, 4, method=method, controller=controller)
