@@ -342,7 +342,11 @@ typedef struct rk_dense_eig_batch {
   int64_t n_inst;        /* instances                                                     */
   int32_t nl_kind;       /* RK_NL_ALLEN_CAHN                                              */
   int32_t err_eigen;     /* 0: physical error vector; 1: eigenbasis error vector          */
-  const double* eig;     /* [device] n real eigenvalues of lin_op                        */
+  const double* eig;     /* [device] n real eigenvalues of lin_op.  err_eigen = 0: any
+                            order gives the same results, descending order balances the
+                            coefficient rebuilds; err_eigen = 1: the order decides which
+                            components the mask keeps (numpy.linalg.eig's order is the
+                            reference's)                                                  */
   const double* S;       /* [device] n x n eigenvectors, row-major                       */
   const double* Sinv;    /* [device] n x n inverse of S, row-major                       */
   const double* shift;   /* [device] n points x of the nonlinearity                      */

@@ -109,11 +109,82 @@ RK_DEV float nl_ac(float w, float x) {
   return x - v * v * v;
 }
 
-// FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): double-float
-// arithmetic up to z = 80 (the psi Taylor series below modecutoff), FP64 beyond; the
-// branches of the diagonal path's FP32 coefficient build.
+// Stiff modes: below z = -STIFF_Z the coefficients are evaluated in FP32 (expf for the
+// exponentials) in a form without cancellation, accurate to a few FP32 ulps.
+constexpr float STIFF_Z = 32.f;
+
+// (a psi_1 + b psi_2 + g psi_3) / D at the scale x = 1/r (h psi_k as the coefficient
+// formulas use them) with e = e^x.  From psi_1 = h r (e - 1), psi_2 = 2 h r^2 (e - 1) - 2 h r
+// and psi_3 = 6 h r^3 (e - 1) - 6 h r^2 - 3 h r:
+//   h r [ -(a + 2b + 3g) - (2b + 6g) r - 6g r^2 + e (a + 2b r + 6g r^2) ] / D,
+// the integer sums exact, so that the leading terms of the combinations (which cancel in
+// the psi form, e.g. psi_1 - psi_2 / 2 ~ r^2) never cancel in FP32; |r| <= 1/8 here.
+template <int A, int B, int G, int D>
+RK_DEV float stiff_comb(float h, float r, float e) {
+  constexpr float k1 = -(float)(A + 2 * B + 3 * G) / (float)D, k2 = -(float)(2 * B + 6 * G) / (float)D;
+  constexpr float k3 = -(float)(6 * G) / (float)D;
+  constexpr float m0 = (float)A / (float)D, m1 = (float)(2 * B) / (float)D, m2 = (float)(6 * G) / (float)D;
+  return (h * r) * ((k1 + r * (k2 + r * k3)) + e * (m0 + r * (m1 + r * m2)));
+}
+
+// FP32 coefficients of a stiff real mode (z < -STIFF_Z): the combinations of etd_from_psi_e
+// (etd35.py:157-288, etd34.py:107-149, if34.py:109-112) through stiff_comb.
+template <int METHOD>
+RK_DEV void stiff_coeffs_f32(float z, float h, float* o) {
+  if constexpr (METHOD == RK_IF34) {
+    o[CIF_E] = expf(z);
+    o[CIF_E2] = expf(0.5f * z);
+  } else {
+    const float e1 = expf(0.25f * z), e2 = e1 * e1, e4 = e2 * e2;
+    const float rz = 1.f / z;
+    if constexpr (METHOD == RK_ETD35) {
+      const float e3 = e2 * e1, r14 = 4.f * rz, r12 = 2.f * rz, r34 = rz * (4.f / 3.f);
+      o[C35_E14] = e1;
+      o[C35_E12] = e2;
+      o[C35_E34] = e3;
+      o[C35_E] = e4;
+      o[C35_A21] = stiff_comb<1, 0, 0, 4>(h, r14, e1);
+      o[C35_A31] = stiff_comb<2, -1, 0, 8>(h, r14, e1);
+      o[C35_A32] = stiff_comb<0, 1, 0, 8>(h, r14, e1);
+      o[C35_A41] = stiff_comb<1, -1, 0, 2>(h, r12, e2);
+      o[C35_A43] = stiff_comb<0, 1, 0, 2>(h, r12, e2);
+      o[C35_A51] = stiff_comb<12, -9, 0, 16>(h, r34, e3);
+      o[C35_A52] = stiff_comb<-3, 0, 0, 8>(h, r34, e3);
+      o[C35_A54] = stiff_comb<0, 9, 0, 16>(h, r34, e3);
+      o[C35_A61] = stiff_comb<-77, 59, 0, 42>(h, rz, e4);
+      o[C35_A62] = stiff_comb<8, 0, 0, 7>(h, rz, e4);
+      o[C35_A63] = stiff_comb<111, -87, 0, 28>(h, rz, e4);
+      o[C35_A65] = stiff_comb<-47, 143, 0, 84>(h, rz, e4);
+      o[C35_A71] = stiff_comb<1799, -3479, 1890, 2700>(h, rz, e4);
+      o[C35_A73] = stiff_comb<1097, -467, -150, 1350>(h, rz, e4);
+      o[C35_A74] = stiff_comb<-98, 398, -270, 225>(h, rz, e4);
+      o[C35_A75] = stiff_comb<-313, 883, -90, 1350>(h, rz, e4);
+      o[C35_A76] = stiff_comb<509, -2129, 1830, 2700>(h, rz, e4);
+    } else {
+      const float r12 = 2.f * rz;
+      o[C34_E] = e4;
+      o[C34_E2] = e2;
+      o[C34_A21] = stiff_comb<1, 0, 0, 2>(h, r12, e2);
+      o[C34_A31] = stiff_comb<1, -1, 0, 2>(h, r12, e2);
+      o[C34_A32] = stiff_comb<0, 1, 0, 2>(h, r12, e2);
+      o[C34_A41] = stiff_comb<1, -1, 0, 1>(h, rz, e4);
+      o[C34_A43] = stiff_comb<0, 1, 0, 1>(h, rz, e4);
+      o[C34_A51] = stiff_comb<6, -9, 4, 6>(h, rz, e4);
+      o[C34_A52] = stiff_comb<0, 3, -2, 3>(h, rz, e4);
+      o[C34_A54] = stiff_comb<0, -3, 4, 6>(h, rz, e4);
+    }
+  }
+}
+
+// FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): FP32 below
+// z = -STIFF_Z, double-float arithmetic up to z = 80 (the psi Taylor series below
+// modecutoff), FP64 beyond.
 template <int METHOD>
 RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
+  if (z < -(double)STIFF_Z) {
+    stiff_coeffs_f32<METHOD>((float)z, (float)h, out);
+    return;
+  }
   if constexpr (METHOD == RK_IF34) {
     // e^z and e^(z/2) (if34.py:109-112)
     if (z <= 80.0) {
@@ -139,7 +210,7 @@ RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
   }
 }
 template <int METHOD> __host__ __device__ constexpr int num_coeffs() {
-  return METHOD == RK_ETD35 ? C35_N : METHOD == RK_ETD34 ? C34_N : CIF_N;
+  return METHOD == RK_ETD35 ? (int)C35_N : METHOD == RK_ETD34 ? (int)C34_N : (int)CIF_N;
 }
 
 // Element (instance j, K row `row`) of the stage operand in shared memory: the tile of the
@@ -296,6 +367,9 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
   int* need = reinterpret_cast<int*>(hsm + NT);                          // [NT] coefficients to rebuild
   int* acc_ok = need + NT;                                               // [NT] attempt accepted
   int* running = acc_ok + NT;                                            // [NT] instance running
+  int* stiffq = running + NT;  // [NT] bit q: every row of chunk q of the instance is stiff at its h
+  double* lamq = reinterpret_cast<double*>(stiffq + NT);                 // [4] largest eig of each chunk
+  unsigned* needw = reinterpret_cast<unsigned*>(lamq + DM / 32);         // [2] need[] as a bit mask
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t col0 = (int64_t)blockIdx.x * NT;
@@ -314,6 +388,11 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     tc::mbar_init(xb, EPI_THREADS);
     flags[0] = 0;
     flags[1] = 0;
+    for (int q = 0; q < DM / 32; ++q) {
+      double m = p.eig[q * 32];
+      for (int r = q * 32 + 1; r < q * 32 + 32; ++r) m = fmax(m, p.eig[r]);
+      lamq[q] = m;
+    }
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tmA);
   }
@@ -401,7 +480,6 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     const int row = tid & (DM - 1), ch = tid >> 7, quarter = warp & 3;
     const int j0 = ch * 32;
     const float xr = p.shift[row];
-    const double lam = p.eig[row];
     const bool own = tid < NT && col0 + tid < p.n_inst;
     rk_inst_state so{};
     if (own) so = p.st[col0 + tid];
@@ -446,7 +524,13 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
       if (tid < NT) {
         running[tid] = own && so.status == RK_ST_RUNNING;
         hsm[tid] = own ? so.h : 0.0;
-        need[tid] = own && so.status == RK_ST_RUNNING && so.h != so.h_coeff;  // exact, as etd35.py:851
+        const bool nd = own && so.status == RK_ST_RUNNING && so.h != so.h_coeff;  // exact, as etd35.py:851
+        need[tid] = nd;
+        const unsigned b = __ballot_sync(0xffffffffu, nd);  // warps 0 and 1, all lanes
+        if (lane == 0) needw[warp] = b;
+        int m = 0;
+        for (int q = 0; q < DM / 32; ++q) m |= (hsm[tid] * lamq[q] < -(double)STIFF_Z) ? (1 << q) : 0;
+        stiffq[tid] = m;
       }
     };
     // decision 0
@@ -562,20 +646,40 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
       return true;
     };
     for (int a = 0; ok && !stop0; ++a) {
-      // coefficients of the instances whose h changed (this thread's mode and instances)
-      for (int jj = 0; jj < 32; ++jj) {
-        const int j = j0 + jj;
-        if (!need[j]) continue;
-        float c[NCF];
-        const double h = hsm[j];
-        mode_coeffs_f32<METHOD>(h * lam, h, p.ec, c);
-        float* cp = p.C + ((col0 + j) * C35_N) * DM + row;
+      // Coefficients of the instances whose h changed, in units of (instance j, 32-row chunk
+      // q) dealt round-robin to the eight epilogue warps: first the units with a row that is
+      // not stiff (double-float psi functions), then the all-stiff ones (FP32), so that every
+      // warp gets a like share of the slow work.  Lane l computes row 32 q + l; each value
+      // depends only on its own h lambda, whichever warp computes it.
+      const unsigned long long nmask = (unsigned long long)needw[0] | ((unsigned long long)needw[1] << 32);
+      if (nmask) {
+        int u = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+          for (unsigned long long mk = nmask; mk; mk &= mk - 1) {
+            const int j = __ffsll((long long)mk) - 1;
+            const int sq = stiffq[j];
+            for (int q = 0; q < DM / 32; ++q) {
+              if (((sq >> q) & 1) != pass) continue;
+              if ((u++ & (EPI_WARPS - 1)) != warp) continue;
+              const int r = q * 32 + lane;
+              float c[NCF];
+              const double h = hsm[j];
+              mode_coeffs_f32<METHOD>(h * p.eig[r], h, p.ec, c);
+              float* cp = p.C + ((col0 + j) * C35_N) * DM + r;
 #pragma unroll
-        for (int k = 0; k < NCF; ++k) cp[k * DM] = c[k];
+              for (int k = 0; k < NCF; ++k) cp[k * DM] = c[k];
+            }
+          }
+        }
       }
       if (own && need[tid]) {
         so.h_coeff = so.h;
         so.coeff_updates += 1;
+      }
+      if (nmask) {
+        // the coefficients written by other warps, visible before the stages read them
+        __threadfence_block();
+        if (!(ok = sync_epi())) break;
       }
       bool stop = false;
       if constexpr (METHOD == RK_ETD35) {

@@ -80,6 +80,14 @@ class DenseEnsemble:
             if np.max(np.abs(w.imag)) > 1e-12 * max(1.0, np.max(np.abs(w))):
                 raise NotImplementedError("the dense path needs an operator with a real spectrum")
             w, S = w.real, S.real
+        if not self.err_eigen:
+            # eigenvalues in descending order: the stiff modes of every h fill whole 32-row
+            # chunks, which balances the per-instance kernel's coefficient rebuilds.  The
+            # eigenbasis error vector keeps NumPy's order: the reference masks it by the
+            # physical state's index (etd35.py:495 into solveras.py:412-455), so the order
+            # of the eigenvectors decides which components count.
+            order = np.argsort(-w, kind="stable")
+            w, S = w[order], S[:, order]
         Sinv = np.linalg.inv(S)
         self.lib = nat.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
