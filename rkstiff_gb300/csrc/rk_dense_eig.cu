@@ -128,17 +128,26 @@ RK_DEV float stiff_comb(float h, float r, float e) {
 }
 
 // FP32 coefficients of a stiff real mode (z < -STIFF_Z): the combinations of etd_from_psi_e
-// (etd35.py:157-288, etd34.py:107-149, if34.py:109-112) through stiff_comb.
+// (etd35.py:157-288, etd34.py:107-149, if34.py:109-112) through stiff_comb.  z = zf + zl
+// with zf its FP32 rounding: each exponential e^(c z) = e^(c zf) (1 + c zl) and 1/z =
+// (1/zf)(1 - zl/zf) to first order in zl (|zl| <= 2^-24 |z|), so that neither takes the
+// rounding of z (an error of |c z| 2^-24 relative in e^(c z)).
 template <int METHOD>
-RK_DEV void stiff_coeffs_f32(float z, float h, float* o) {
+RK_DEV void stiff_coeffs_f32(double zd, double hd, float* o) {
+  const float zf = (float)zd, zl = (float)(zd - (double)zf), h = (float)hd;
+  auto ex = [&](float c) {  // e^(c z) for c = 1/4, 1/2, 1 (c zf exact)
+    const float e = expf(c * zf);
+    return fmaf(e, c * zl, e);
+  };
   if constexpr (METHOD == RK_IF34) {
-    o[CIF_E] = expf(z);
-    o[CIF_E2] = expf(0.5f * z);
+    o[CIF_E] = ex(1.f);
+    o[CIF_E2] = ex(0.5f);
   } else {
-    const float e1 = expf(0.25f * z), e2 = e1 * e1, e4 = e2 * e2;
-    const float rz = 1.f / z;
+    const float e2 = ex(0.5f), e4 = ex(1.f);
+    float rz = 1.f / zf;
+    rz = fmaf(-(zl * rz), rz, rz);
     if constexpr (METHOD == RK_ETD35) {
-      const float e3 = e2 * e1, r14 = 4.f * rz, r12 = 2.f * rz, r34 = rz * (4.f / 3.f);
+      const float e1 = ex(0.25f), e3 = e2 * e1, r14 = 4.f * rz, r12 = 2.f * rz, r34 = rz * (4.f / 3.f);
       o[C35_E14] = e1;
       o[C35_E12] = e2;
       o[C35_E34] = e3;
@@ -182,7 +191,7 @@ RK_DEV void stiff_coeffs_f32(float z, float h, float* o) {
 template <int METHOD>
 RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
   if (z < -(double)STIFF_Z) {
-    stiff_coeffs_f32<METHOD>((float)z, (float)h, out);
+    stiff_coeffs_f32<METHOD>(z, h, out);
     return;
   }
   if constexpr (METHOD == RK_IF34) {

@@ -19,6 +19,7 @@ Tolerances (the same FP32-stage bounds as the lockstep path):
 
 import numpy as np
 import pytest
+import torch
 
 from oracle import rk_oracle as O
 from rkstiff_gb300 import _native as nat
@@ -256,3 +257,50 @@ def test_if34_config5_reaches_tf(err_basis):
         err = np.linalg.norm(out[i] - ref) / np.linalg.norm(ref)
         print(f"IF34 ({err_basis}) instance {i}: rel L2 vs FP64 {err:.3e}, attempts {st['attempts'][i]} vs {s.attempts}")
         assert err <= 2e-3, (i, err)
+
+
+@pytest.mark.parametrize("method", ["ETD35", "ETD34", "IF34"])
+def test_instance_coefficients_round_fp64(method):
+    """The kernel's FP32 coefficient block (read back from its work buffer after one
+    attempt) against the diagonal path's FP64 coefficients of the same h lambda rounded to
+    FP32, over the Allen-Cahn spectrum at h from 3e-3 to 9 (z from +9 to -1.2e6): within 8
+    FP32 ulps for |z| >= modecutoff (FP32 below z = -32 through the cancellation-free
+    grouping, double-float above), the small modes (Taylor series here, the contour mean in
+    FP64) within 1e-6 of the array's scale."""
+    from test_gpu_parity import device_coeffs
+
+    x, (lin, nl) = ac_ops(129)
+    xi = x[1:-1]
+    n = xi.size
+    hs = [0.003, 0.05, 0.7, 9.0]
+    ens = DenseEnsemble(lin, nl, len(hs), config=SolverConfig(epsilon=1e-3), controller="instance", method=method)
+    u = ens.pack_u(ics(len(hs), 4, xi, 0.05))
+    st = ens.fresh_state(0.0, 100.0, 0.1)
+    st["h"] = hs
+    ens.put_state(st)
+    st = ens.run(u, 1)
+    assert np.all(st["coeff_updates"] == 1)
+    # work buffer: S / S^-1 hi-lo block, the [3][bpad][128] vectors, then C[bpad][21][128]
+    dm, bpad = nat.RK_DENSE_NMAX, 64
+    off_c = ((2 * 2 * dm * dm * 4 + 3 * bpad * dm * 4) + 1023) // 1024 * 1024
+    base = ens.work_ptr - ens._work_buf.data_ptr()
+    blk = ens._work_buf[base + off_c: base + off_c + bpad * 21 * dm * 4].view(torch.float32)
+    blk = blk.reshape(bpad, 21, dm).cpu().numpy().astype(np.float64)
+    w = ens.eig.cpu().numpy()
+    nc = {"ETD35": 21, "ETD34": 10, "IF34": 2}[method]
+    worst = 0.0
+    for i, h in enumerate(hs):
+        c64 = device_coeffs(method, w, h, nat.RK_FP64).real
+        c32 = blk[i, :nc, :n]
+        r32 = c64.astype(np.float32).astype(np.float64)
+        ulp = np.spacing(np.abs(r32).astype(np.float32)).astype(np.float64)
+        direct = np.abs(h * w) >= 0.01
+        d = np.abs(c32 - r32)[:, direct] / np.maximum(ulp[:, direct], 1e-45)
+        worst = max(worst, float(d.max()))
+        bad = d > 8
+        assert not np.any(bad), (method, h, np.argwhere(bad)[:3])
+        small = ~direct
+        if np.any(small):
+            scale = np.max(np.abs(c64), axis=1)
+            assert np.all(np.max(np.abs(c32 - c64)[:, small], axis=1) <= 1e-6 * scale), (method, h)
+    print(f"{method}: dense per-instance coefficients within {worst:.1f} FP32 ulps of FP64")
