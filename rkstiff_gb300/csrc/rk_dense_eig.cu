@@ -605,53 +605,53 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     // cutoff^2 max |u|^2.  Rows: the 32 lanes of a warp (reduce-scatter: lane l ends with
     // instance j0 + l) and the four lane quarters (shared memory).
     auto error_test = [&](int a, bool& stop) -> bool {
-        warp_reduce_scatter32(u2, lane, [](float x, float y) { return fmaxf(x, y); });
-        red[(0 * 4 + quarter) * NT + j0 + lane] = u2[0];
-        if (!sync_epi()) return false;
-        const float cut2 = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff);
-  #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          const int j = j0 + jj;
-          const float mx = fmaxf(fmaxf(red[j], red[NT + j]), fmaxf(red[2 * NT + j], red[3 * NT + j]));
-          const float up = acc[jj], a2 = up * up;
-          const bool m = a2 > cut2 * mx;
-          u2[jj] = m ? a2 : 0.f;
-          e2[jj] = m ? e2[jj] : 0.f;
-        }
-        warp_reduce_scatter32(u2, lane, [](float x, float y) { return x + y; });
-        warp_reduce_scatter32(e2, lane, [](float x, float y) { return x + y; });
-        red[(1 * 4 + quarter) * NT + j0 + lane] = u2[0];
-        red[(2 * 4 + quarter) * NT + j0 + lane] = e2[0];
-        if (!sync_epi()) return false;
-        if (tid < NT) {
-          acc_ok[tid] = 0;
-          if (own && so.status == RK_ST_RUNNING) {
-            double su = 0.0, se = 0.0;
-            for (int w = 0; w < 4; ++w) {
-              su += (double)red[(1 * 4 + w) * NT + tid];
-              se += (double)red[(2 * 4 + w) * NT + tid];
-            }
-            // s = safety (eps |u| / |err|)^(1/q), q = 4, as ratio^(1/8) of ratio = eps^2 su / se.
-            // An error vector that is exactly zero in FP32 while |u| > 0 (IF34's h (N4 - N5) / 6
-            // on a short last step) lies below FP32 resolution: the largest growth, MAX_S = 4,
-            // instead of the rejection x/0 = inf would give.
-            const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
-            const double sv = (se == 0.0 && su > 0.0 && !isinf(su)) ? 4.0
-                              : (ratio != ratio || isinf(ratio)) ? p.ctl.safety_f * ratio
-                                                                 : p.ctl.safety_f * pow(ratio, 0.125);
-            acc_ok[tid] = control_instance(so, sv, p.ctl, METHOD != RK_ETD35);
+      warp_reduce_scatter32(u2, lane, [](float x, float y) { return fmaxf(x, y); });
+      red[(0 * 4 + quarter) * NT + j0 + lane] = u2[0];
+      if (!sync_epi()) return false;
+      const float cut2 = (float)(p.ctl.adapt_cutoff * p.ctl.adapt_cutoff);
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) {
+        const int j = j0 + jj;
+        const float mx = fmaxf(fmaxf(red[j], red[NT + j]), fmaxf(red[2 * NT + j], red[3 * NT + j]));
+        const float up = acc[jj], a2 = up * up;
+        const bool m = a2 > cut2 * mx;
+        u2[jj] = m ? a2 : 0.f;
+        e2[jj] = m ? e2[jj] : 0.f;
+      }
+      warp_reduce_scatter32(u2, lane, [](float x, float y) { return x + y; });
+      warp_reduce_scatter32(e2, lane, [](float x, float y) { return x + y; });
+      red[(1 * 4 + quarter) * NT + j0 + lane] = u2[0];
+      red[(2 * 4 + quarter) * NT + j0 + lane] = e2[0];
+      if (!sync_epi()) return false;
+      if (tid < NT) {
+        acc_ok[tid] = 0;
+        if (own && so.status == RK_ST_RUNNING) {
+          double su = 0.0, se = 0.0;
+          for (int w = 0; w < 4; ++w) {
+            su += (double)red[(1 * 4 + w) * NT + tid];
+            se += (double)red[(2 * 4 + w) * NT + tid];
           }
+          // s = safety (eps |u| / |err|)^(1/q), q = 4, as ratio^(1/8) of ratio = eps^2 su / se.
+          // An error vector that is exactly zero in FP32 while |u| > 0 (IF34's h (N4 - N5) / 6
+          // on a short last step) lies below FP32 resolution: the largest growth, MAX_S = 4,
+          // instead of the rejection x/0 = inf would give.
+          const double ratio = (p.ctl.epsilon * p.ctl.epsilon * su) / se;
+          const double sv = (se == 0.0 && su > 0.0 && !isinf(su)) ? 4.0
+                            : (ratio != ratio || isinf(ratio)) ? p.ctl.safety_f * ratio
+                                                               : p.ctl.safety_f * pow(ratio, 0.125);
+          acc_ok[tid] = control_instance(so, sv, p.ctl, METHOD != RK_ETD35);
         }
-        publish_state();
-        if (!sync_epi()) return false;
-        if (tid == 0) {
-          int any = 0;
-          for (int j = 0; j < NT; ++j) any |= running[j];
-          flags[0] = (!any || a + 1 >= p.max_attempts) ? 1 : 0;
-        }
-        if (!sync_epi()) return false;
-        stop = flags[0] != 0;
-        tc::mbar_arrive(go);
+      }
+      publish_state();
+      if (!sync_epi()) return false;
+      if (tid == 0) {
+        int any = 0;
+        for (int j = 0; j < NT; ++j) any |= running[j];
+        flags[0] = (!any || a + 1 >= p.max_attempts) ? 1 : 0;
+      }
+      if (!sync_epi()) return false;
+      stop = flags[0] != 0;
+      tc::mbar_arrive(go);
       return true;
     };
     for (int a = 0; ok && !stop0; ++a) {
@@ -693,13 +693,13 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
       bool stop = false;
       if constexpr (METHOD == RK_ETD35) {
         // k2 = E14 v + a21 N1 (etd35.py:320)
-  #pragma unroll
+#pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           float v[16], n1[16];
           tld(T_V, sub, v);
           tld(T_N1, sub, n1);
           tc::tmem_ld_wait();
-  #pragma unroll
+#pragma unroll
           for (int k = 0; k < 16; ++k) {
             const int j = j0 + sub * 16 + k;
             dep_put(dep, row, j, cf(j, C35_E14) * v[k] + cf(j, C35_A21) * n1[k]);
@@ -712,11 +712,11 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
           constexpr int st = decltype(stc)::value;
           if (!wait_acc()) return false;
           load_acc();
-  #pragma unroll
+#pragma unroll
           for (int jj = 0; jj < 32; ++jj) dep_put(dep, row, j0 + jj, nl_ac(acc[jj], xr));
           publish();
           if (!wait_acc()) return false;
-  #pragma unroll
+#pragma unroll
           for (int sub = 0; sub < 2; ++sub) {
             float nk[16], v[16], n1[16], x1[16], x2[16], x3[16];
             tld(T_ACC, sub, nk);
@@ -735,7 +735,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
               tld(T_N5, sub, x3);
             }
             tc::tmem_ld_wait();
-  #pragma unroll
+#pragma unroll
             for (int k = 0; k < 16; ++k) {
               const int j = j0 + sub * 16 + k;
               // etd35.py:322-345
@@ -777,22 +777,22 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
           publish();
           if (!(ok = wait_acc())) break;
           load_acc();
-  #pragma unroll
+#pragma unroll
           for (int jj = 0; jj < 32; ++jj) e2[jj] = acc[jj] * acc[jj];
         }
-  #pragma unroll
+#pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           float un[16];
           tld(T_UN, sub, un);
           tc::tmem_ld_wait();
-  #pragma unroll
+#pragma unroll
           for (int k = 0; k < 16; ++k) dep_put(dep, row, j0 + sub * 16 + k, un[k]);
         }
         publish();
         if (!(ok = wait_acc())) break;
         // S unew: the physical new state; N(S unew) for the next attempt's N1
         load_acc();
-  #pragma unroll
+#pragma unroll
         for (int jj = 0; jj < 32; ++jj) {
           const float up = acc[jj];
           const float a2 = up * up;
@@ -802,11 +802,11 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
         publish();
         if (!(ok = error_test(a, stop))) break;
         // the physical new state is in acc until the next load; keep it in u2 for the update
-  #pragma unroll
+#pragma unroll
         for (int jj = 0; jj < 32; ++jj) u2[jj] = acc[jj];
         if (!(ok = wait_acc())) break;
         // accepted instances take the new state and N1 = S^-1 N(S unew)
-  #pragma unroll
+#pragma unroll
         for (int sub = 0; sub < 2; ++sub) {
           float n1n[16], n1[16], v[16], un[16];
           tld(T_ACC, sub, n1n);
@@ -814,7 +814,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
           tld(T_V, sub, v);
           tld(T_UN, sub, un);
           tc::tmem_ld_wait();
-  #pragma unroll
+#pragma unroll
           for (int k = 0; k < 16; ++k) {
             const int j = j0 + sub * 16 + k;
             if (acc_ok[j]) {
