@@ -435,6 +435,22 @@ RK_DEV double write_unew(const Ctx<T, CT, LOGN>& x, KF kf) {
   }
 }
 
+// s from the masked sums su = sum |u|^2, se = sum |err|^2 in FP32 working precision:
+// (eps |u| / |err|)^(1/q) = ratio^(1/(2q)) with ratio = eps^2 su / se formed in FP64; the
+// fractional power runs in FP32 (FP64 pow is a long dependent chain on this GPU).  Edge
+// values keep the reference's outcome: 0/0 -> NaN and x/0 -> inf (both rejected), a finite
+// ratio beyond FP32 range stays finite (accepted).  The one exception: an error vector that
+// is exactly zero in FP32 while |u| > 0 lies below FP32 resolution (an FP64 error of the same
+// attempt is small but not zero), so the attempt takes the largest growth, MAX_S = 4,
+// instead of the rejection that x/0 = inf would give.
+RK_DEV double s_from_sums_f32(double su, double se, const rk_controller& ctl, int q) {
+  if (se == 0.0 && su > 0.0 && !isinf(su)) return 4.0;
+  const double ratio = (ctl.epsilon * ctl.epsilon * su) / se;
+  if (ratio != ratio || isinf(ratio)) return ctl.safety_f * ratio;
+  const float rf = (float)fmin(ratio, 1e30);
+  return ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / (float)q));
+}
+
 // s = safety (eps |unew[mask]| / |err[mask]|)^(1/q), mask = |unew| / max|unew| > cutoff
 // (rkstiff/solveras.py:451-455).  The sums of squares are accumulated in FP64.  In FP32
 // working precision the mask is evaluated on squared magnitudes, |u|^2 > cutoff^2 max|u|^2,
@@ -474,19 +490,45 @@ RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const 
     double tol = ctl.epsilon * sqrt(su);
     return ctl.safety_f * pow(tol / sqrt(se), 1.0 / q);
   } else {
-    // (eps |u| / |err|)^(1/q) = ratio^(1/(2q)) with ratio = eps^2 su / se formed in FP64;
-    // the fractional power runs in FP32 (FP64 pow is a long dependent chain on this GPU).
-    // Edge values keep the reference's outcome: 0/0 -> NaN and x/0 -> inf (both rejected),
-    // a finite ratio beyond FP32 range stays finite (accepted).  The one exception: an error
-    // vector that is exactly zero in FP32 while |u| > 0 lies below FP32 resolution (an FP64
-    // error of the same attempt is small but not zero), so the attempt takes the largest
-    // growth, MAX_S = 4, instead of the rejection that x/0 = inf would give.
-    if (se == 0.0 && su > 0.0 && !isinf(su)) return 4.0;
-    double ratio = (ctl.epsilon * ctl.epsilon * su) / se;
-    if (ratio != ratio || isinf(ratio)) return ctl.safety_f * ratio;
-    float rf = (float)fmin(ratio, 1e30);
-    return ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / (float)q));
+    return s_from_sums_f32(su, se, ctl, q);
   }
+}
+
+// ETD35 in FP32 working precision: unew and |err|^2 in one pass over the modes (the error
+// combination reads the same stage vectors as unew), |unew|^2 and |err|^2 of each mode
+// parked in the FFT buffer (free between attempts) until the group maximum of |unew|^2 is
+// known; then the masked sums from those two floats per mode.  Same values as write_unew
+// followed by controller_s, without the second pass over the stage vectors.
+template <class T, class CT, int LOGN, class KF, class EF>
+RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const rk_controller& ctl, int q) {
+  float* park = reinterpret_cast<float*>(x.fa);  // [2 m] floats: the buffer holds >= n complex
+  x.g.sync();  // the last transform has released the buffer
+  float mx = 0.f;
+  bool nan = false;
+  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+    const cx<T> v = kf(j);
+    const cx<T> e = ef(j);
+    x.unew[j] = v;
+    const float a2 = v.x * v.x + v.y * v.y;
+    if (a2 != a2) nan = true;
+    else mx = fmaxf(mx, a2);
+    park[2 * j] = a2;
+    park[2 * j + 1] = e.x * e.x + e.y * e.y;
+  }
+  const double maxu = (double)group_max_nan_f(x.g, x.red, mx, nan);
+  // NaN keeps every comparison false, as in the reference
+  const float thr = (float)(ctl.adapt_cutoff * ctl.adapt_cutoff * maxu);
+  df au{0.f, 0.f}, ae{0.f, 0.f};
+  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+    const float a2 = park[2 * j];
+    if (a2 > thr) {
+      au = df_add(au, a2);
+      ae = df_add(ae, park[2 * j + 1]);
+    }
+  }
+  double su = 0.0, se = 0.0;
+  group_sum2_df(x.g, x.red, au, ae, su, se);
+  return s_from_sums_f32(su, se, ctl, q);
 }
 
 // ---------------------------------------------------------------------------------
@@ -528,11 +570,16 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
     nl_count += 1;
     return 0.0;
   }
-  double mx = write_unew(x, k7);
-  return controller_s(x, mx, [&](int j) {
+  auto err = [&](int j) {
     cx<T> s = (((-N[0][j] + T(4) * N[2][j]) - T(6) * N[3][j]) + T(4) * N[4][j]) - N[5][j];
     return cmul(x.c(C35_A75, j), s);
-  }, ctl, 4);
+  };
+  if constexpr (sizeof(T) == sizeof(float)) {
+    return unew_and_s_f32(x, k7, err, ctl, 4);
+  } else {
+    double mx = write_unew(x, k7);
+    return controller_s(x, mx, err, ctl, 4);
+  }
 }
 
 template <class T, class CT, int LOGN>
