@@ -224,4 +224,81 @@ RK_DEV void dd_etd_coeffs(int method, double zd, dd h, float* o, bool small = fa
   }
 }
 
+// Stiff modes: below z = -STIFF_Z the coefficients are evaluated in FP32 (expf for the
+// exponentials) in a form without cancellation, accurate to a few FP32 ulps.
+constexpr float STIFF_Z = 32.f;
+
+// (a psi_1 + b psi_2 + g psi_3) / D at the scale x = 1/r (h psi_k as the coefficient
+// formulas use them) with e = e^x.  From psi_1 = h r (e - 1), psi_2 = 2 h r^2 (e - 1) - 2 h r
+// and psi_3 = 6 h r^3 (e - 1) - 6 h r^2 - 3 h r:
+//   h r [ -(a + 2b + 3g) - (2b + 6g) r - 6g r^2 + e (a + 2b r + 6g r^2) ] / D,
+// the integer sums exact, so that the leading terms of the combinations (which cancel in
+// the psi form, e.g. psi_1 - psi_2 / 2 ~ r^2) never cancel in FP32; |r| <= 1/8 here.
+template <int A, int B, int G, int D>
+RK_DEV float stiff_comb(float h, float r, float e) {
+  constexpr float k1 = -(float)(A + 2 * B + 3 * G) / (float)D, k2 = -(float)(2 * B + 6 * G) / (float)D;
+  constexpr float k3 = -(float)(6 * G) / (float)D;
+  constexpr float m0 = (float)A / (float)D, m1 = (float)(2 * B) / (float)D, m2 = (float)(6 * G) / (float)D;
+  return (h * r) * ((k1 + r * (k2 + r * k3)) + e * (m0 + r * (m1 + r * m2)));
+}
+
+// FP32 coefficients of a stiff real mode (z < -STIFF_Z), layouts C35_* (ETD35, ETD5), C34_*
+// (ETD34, ETD4) and CIF_* (IF34): the combinations of etd_from_psi_e (etd35.py:157-288,
+// etd34.py:107-149, if34.py:109-112) through stiff_comb.  z = zf + zl
+// with zf its FP32 rounding: each exponential e^(c z) = e^(c zf) (1 + c zl) and 1/z =
+// (1/zf)(1 - zl/zf) to first order in zl (|zl| <= 2^-24 |z|), so that neither takes the
+// rounding of z (an error of |c z| 2^-24 relative in e^(c z)).
+template <int METHOD>
+RK_DEV void stiff_coeffs_f32(double zd, double hd, float* o) {
+  const float zf = (float)zd, zl = (float)(zd - (double)zf), h = (float)hd;
+  auto ex = [&](float c) {  // e^(c z) for c = 1/4, 1/2, 1 (c zf exact)
+    const float e = expf(c * zf);
+    return fmaf(e, c * zl, e);
+  };
+  if constexpr (METHOD == RK_IF34) {
+    o[CIF_E] = ex(1.f);
+    o[CIF_E2] = ex(0.5f);
+  } else {
+    const float e2 = ex(0.5f), e4 = ex(1.f);
+    float rz = 1.f / zf;
+    rz = fmaf(-(zl * rz), rz, rz);
+    if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) {
+      const float e1 = ex(0.25f), e3 = e2 * e1, r14 = 4.f * rz, r12 = 2.f * rz, r34 = rz * (4.f / 3.f);
+      o[C35_E14] = e1;
+      o[C35_E12] = e2;
+      o[C35_E34] = e3;
+      o[C35_E] = e4;
+      o[C35_A21] = stiff_comb<1, 0, 0, 4>(h, r14, e1);
+      o[C35_A31] = stiff_comb<2, -1, 0, 8>(h, r14, e1);
+      o[C35_A32] = stiff_comb<0, 1, 0, 8>(h, r14, e1);
+      o[C35_A41] = stiff_comb<1, -1, 0, 2>(h, r12, e2);
+      o[C35_A43] = stiff_comb<0, 1, 0, 2>(h, r12, e2);
+      o[C35_A51] = stiff_comb<12, -9, 0, 16>(h, r34, e3);
+      o[C35_A52] = stiff_comb<-3, 0, 0, 8>(h, r34, e3);
+      o[C35_A54] = stiff_comb<0, 9, 0, 16>(h, r34, e3);
+      o[C35_A61] = stiff_comb<-77, 59, 0, 42>(h, rz, e4);
+      o[C35_A62] = stiff_comb<8, 0, 0, 7>(h, rz, e4);
+      o[C35_A63] = stiff_comb<111, -87, 0, 28>(h, rz, e4);
+      o[C35_A65] = stiff_comb<-47, 143, 0, 84>(h, rz, e4);
+      o[C35_A71] = stiff_comb<1799, -3479, 1890, 2700>(h, rz, e4);
+      o[C35_A73] = stiff_comb<1097, -467, -150, 1350>(h, rz, e4);
+      o[C35_A74] = stiff_comb<-98, 398, -270, 225>(h, rz, e4);
+      o[C35_A75] = stiff_comb<-313, 883, -90, 1350>(h, rz, e4);
+      o[C35_A76] = stiff_comb<509, -2129, 1830, 2700>(h, rz, e4);
+    } else {
+      const float r12 = 2.f * rz;
+      o[C34_E] = e4;
+      o[C34_E2] = e2;
+      o[C34_A21] = stiff_comb<1, 0, 0, 2>(h, r12, e2);
+      o[C34_A31] = stiff_comb<1, -1, 0, 2>(h, r12, e2);
+      o[C34_A32] = stiff_comb<0, 1, 0, 2>(h, r12, e2);
+      o[C34_A41] = stiff_comb<1, -1, 0, 1>(h, rz, e4);
+      o[C34_A43] = stiff_comb<0, 1, 0, 1>(h, rz, e4);
+      o[C34_A51] = stiff_comb<6, -9, 4, 6>(h, rz, e4);
+      o[C34_A52] = stiff_comb<0, 3, -2, 3>(h, rz, e4);
+      o[C34_A54] = stiff_comb<0, -3, 4, 6>(h, rz, e4);
+    }
+  }
+}
+
 }  // namespace rk

@@ -315,6 +315,14 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     }
     if constexpr (FAST && sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float)) {
       const double zr = sre(z);
+      if (zr < -(double)STIFF_Z) {
+        // stiff: FP32 arithmetic in a form without cancellation (a few FP32 ulps)
+        float of[NC];
+        stiff_coeffs_f32<METHOD>(zr, h, of);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+        continue;
+      }
       if (zr <= 80.0) {
         // double-float on the FP32 pipes; the result rounds to the FP64 evaluation's
         float of[NC];

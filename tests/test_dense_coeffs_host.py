@@ -20,7 +20,7 @@ import pytest
 
 from oracle import rk_oracle as O
 
-SRC = os.path.join(os.path.dirname(__file__), "..", "rkstiff_gb300", "csrc", "rk_dense_eig.cu")
+SRC = os.path.join(os.path.dirname(__file__), "..", "rkstiff_gb300", "csrc", "rk_dd.cuh")
 LINE = re.compile(r"o\[(C35|C34)_(\w+)\] = stiff_comb<(-?\d+), (-?\d+), (-?\d+), (\d+)>\(h, (\w+), (\w+)\);")
 R_SCALE = {"r14": 0.25, "r12": 0.5, "r34": 0.75, "rz": 1.0}
 E_SCALE = {"e1": 0.25, "e2": 0.5, "e3": 0.75, "e4": 1.0}
