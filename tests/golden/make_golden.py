@@ -263,6 +263,9 @@ def dense_cases(out):
         out["ac20_ETD35_diagz_final"] = s.evolve(w0, t0=0, tf=60, store_data=False)
         s = etd34.ETD34(lin, nl, config=SolverConfig(epsilon=1e-4), diagonalize=True)
         out["ac20_ETD34_diagz_final"] = s.evolve(w0, t0=0, tf=10, store_data=False)
+        s = etd34.ETD34(lin, nl, config=SolverConfig(epsilon=1e-4), etd_config=ETDConfig(contour_points=32,
+                                                                                          contour_radius=10))
+        out["ac20_ETD34_nondiag_final"] = s.evolve(w0, t0=0, tf=10, store_data=False)
         s = if34.IF34(lin, nl, config=SolverConfig(epsilon=1e-4), diagonalize=True)
         out["ac20_IF34_diagz_final"] = s.evolve(w0, t0=0, tf=10, store_data=False)
         s = if34.IF34(lin, nl, config=SolverConfig(epsilon=1e-4))

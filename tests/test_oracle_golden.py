@@ -196,6 +196,14 @@ def test_dense_allen_cahn(golden):
     assert _close(s.evolve(w0, 0, 60, store_data=False), g["ac20_ETD35_diagz_final"], 1e-9)
     s = O.OracleSolver("ETD34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), diagonalize=True)
     assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_ETD34_diagz_final"], 1e-9)
+    # non-diagonal ETD34: the reference's contour-mean matrices exactly; the eigenbasis
+    # matrices (the dense GPU paths' form) differ by the contour's truncation error at R = 10
+    s = O.OracleSolver("ETD34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), cfg)
+    assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_ETD34_nondiag_final"], 1e-12)
+    n_ref = s.attempts
+    s = O.OracleSolver("ETD34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), cfg, dense_psi="eig")
+    assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_ETD34_nondiag_final"], 3e-4)
+    assert s.attempts == n_ref
     s = O.OracleSolver("IF34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4), diagonalize=True)
     assert _close(s.evolve(w0, 0, 10, store_data=False), g["ac20_IF34_diagz_final"], 1e-9)
     s = O.OracleSolver("IF34", g["ac20_lin"], nl, O.SolverConfig(epsilon=1e-4))
