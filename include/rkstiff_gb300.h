@@ -60,7 +60,11 @@ enum {
   RK_ST_MIN_STEP = 2, /* h < minh after a reject (solveras.py:407-410)                 */
   RK_ST_ITER_CAP = 4, /* the launch's accepted-step bound was hit (resumable)          */
   RK_ST_SNAP_FULL = 5,/* the snapshot buffer filled (resumable)                        */
-  RK_ST_STEP_DONE = 6 /* RK_RUN_STEP: one accepted step was taken                      */
+  RK_ST_STEP_DONE = 6,/* RK_RUN_STEP: one accepted step was taken                      */
+  RK_ST_BAD_SIZE = 7, /* the instance's n[i] is not a power of two in [4, n_max] (or not the
+                         size of its class); the instance was not stepped               */
+  RK_ST_WAIT_TIMEOUT = 8 /* rk_dense_eig_evolve: a bounded device wait ran out; the
+                            instances of that CTA stopped where they were             */
 };
 
 /* error codes */
@@ -105,7 +109,10 @@ typedef struct rk_inst_state {
 
 /* One batched run over independent diagonal-operator instances.
  * Modes of instance i live at [mode_off[i], mode_off[i] + m_i) of lin_op / kx / u,
- * m_i = n_i/2 + 1 for RK_NL_UUX (real grid), n_i otherwise. */
+ * m_i = n_i/2 + 1 for RK_NL_UUX (real grid), n_i otherwise.  Every n[i] must be a power of
+ * two with 4 <= n[i] <= n_max (and, with classes, equal to its class's class_n): the kernels
+ * size their shared-memory transforms and, in rk_evolve_noalloc, the scratch slabs from
+ * n_max.  An instance that breaks this is not stepped and ends with RK_ST_BAD_SIZE. */
 typedef struct rk_batch {
   int32_t method;        /* RK_IF34 ... RK_IF4                                        */
   int32_t precision;     /* RK_FP64 / RK_FP32                                         */
@@ -216,14 +223,18 @@ int rk_evolve(const rk_batch* b, void* stream);
 /* No counterpart in the reference.  rk_evolve for callers that cannot allocate device
  * memory -- code running inside another component's CUDA stream capture, plugins whose
  * host application owns every device allocation, hosts that forbid allocation after
- * start-up.  Same batch and results as rk_evolve, but the batch's `slab`, `slab_off` and
+ * start-up.  Same batch and results as rk_evolve (every n[i] <= n_max, as there), but the
+ * batch's `slab`, `slab_off` and
  * `queue` fields are ignored: that scratch is carved from one library-owned device array of
  * RK_NOALLOC_SCRATCH_BYTES (uniform slabs sized for n_max, the offset table and the queue
  * counters), and all instances run as one launch of the runtime-size kernel (no per-size
  * class split, so no side streams are created).  Batches that need more scratch are
- * rejected with RK_E_SIZE.  The call allocates nothing (no cudaMalloc/cudaFree, no stream or
+ * rejected with RK_E_SIZE before anything is launched, as are batches that fail rk_evolve's
+ * argument checks.  The call allocates nothing (no cudaMalloc/cudaFree, no stream or
  * event creation).  The first call on a device looks up the array's device address with
- * cudaGetSymbolAddress, so make that first call before any stream capture.  Every call
+ * cudaGetSymbolAddress, so make that first call before any stream capture; the address is
+ * looked up again only when the device's context changed (after cudaDeviceReset, say), so
+ * do not reset the device between a capture and the graph's replays.  Every call
  * shares the array and it keeps the previous call's contents: the call resets each
  * instance's cached-coefficient key (state[i].h_coeff = NaN) and the queue counters itself,
  * and calls whose work overlaps on the GPU (other streams, other host threads) race on it. */
@@ -364,7 +375,8 @@ typedef struct rk_dense_eig_batch {
 } rk_dense_eig_batch;
 int64_t rk_dense_eig_work_bytes(int64_t n_inst);
 /* Runs until every instance has left RK_ST_RUNNING or made max_attempts attempts; returns
- * after the stream has completed them.  RK_E_CUDA if a device wait timed out. */
+ * after the stream has completed them.  If a bounded device wait ran out, the instances of
+ * that CTA end with status RK_ST_WAIT_TIMEOUT (the call itself still returns 0). */
 int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream);
 
 /* The 3xTF32 tensor-core product of the dense path on its own (no counterpart in the

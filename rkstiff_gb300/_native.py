@@ -22,7 +22,7 @@ RK_FP64, RK_FP32 = 0, 1
 RK_NL_NONE, RK_NL_UUX, RK_NL_NLS, RK_NL_ALLEN_CAHN = 0, 1, 2, 3
 RK_RUN_EVOLVE, RK_RUN_STEP = 0, 1
 RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
-RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE = 4, 5, 6
+RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE, RK_ST_BAD_SIZE, RK_ST_WAIT_TIMEOUT = 4, 5, 6, 7, 8
 RK_OK, RK_E_ARG, RK_E_CUDA, RK_E_UNSUPPORTED, RK_E_SIZE = 0, -1, -2, -3, -4
 RK_TW_N = 8192
 RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL = -1, 0, 1, 2

@@ -152,6 +152,62 @@ static int check_method(int method) {
   return RK_OK;
 }
 
+// Argument checks shared by rk_evolve and rk_evolve_noalloc (the latter passes
+// need_scratch = false: it supplies slab, slab_off and queue itself).  Nothing is launched
+// before these pass.
+int validate_batch(const rk_batch* b, bool need_scratch) {
+  if (!b) {
+    set_error("rk_evolve: null batch");
+    return RK_E_ARG;
+  }
+  if (int e = check_method(b->method)) return e;
+  if (b->precision != RK_FP64 && b->precision != RK_FP32) {
+    set_error("rk_evolve: precision must be RK_FP64 or RK_FP32");
+    return RK_E_ARG;
+  }
+  if (b->nl_kind < RK_NL_NONE || b->nl_kind > RK_NL_NLS) {
+    set_error("rk_evolve: unknown nonlinearity kind");
+    return RK_E_ARG;
+  }
+  if (b->n_inst < 0) {
+    set_error("rk_evolve: negative instance count");
+    return RK_E_ARG;
+  }
+  if (b->n_inst == 0) return RK_OK;
+  if (!b->n || !b->mode_off || !b->lin_op || !b->u || !b->state || !b->twiddle ||
+      (need_scratch && (!b->slab || !b->slab_off || !b->queue))) {
+    set_error("rk_evolve: null device pointer");
+    return RK_E_ARG;
+  }
+  if (b->nl_kind == RK_NL_UUX && !b->kx) {
+    set_error("rk_evolve: RK_NL_UUX needs kx");
+    return RK_E_ARG;
+  }
+  const int nmax = b->n_max;
+  const int limit = b->precision == RK_FP64 ? 4096 : 8192;
+  if (nmax < 4 || (nmax & (nmax - 1)) || nmax > limit) {
+    set_error("rk_evolve: n_max must be a power of two in [4, " + std::to_string(limit) + "]");
+    return RK_E_SIZE;
+  }
+  if (b->store_freq > 0 && (b->snap_cap <= 0 || !b->snap_u || !b->snap_t)) {
+    set_error("rk_evolve: snapshots requested without a snapshot buffer");
+    return RK_E_ARG;
+  }
+  if (b->etd.contour_points < 2) {
+    set_error("rk_evolve: contour_points must be > 1");
+    return RK_E_ARG;
+  }
+  if (b->threads != 0 && b->threads != 32 && b->threads != 64 && b->threads != 128 && b->threads != 256) {
+    set_error("rk_evolve: threads must be 0 (auto), 32, 64, 128 or 256");
+    return RK_E_ARG;
+  }
+  if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_ALL) {
+    set_error("rk_evolve: unknown placement");
+    return RK_E_ARG;
+  }
+  return RK_OK;
+}
+
 }  // namespace rk
 
 using namespace rk;
@@ -212,51 +268,9 @@ int rk_probe_fp32(float* out, int32_t blocks, int32_t threads, int32_t iters, vo
 }
 
 int rk_evolve(const rk_batch* b, void* stream) {
-  if (!b) {
-    set_error("rk_evolve: null batch");
-    return RK_E_ARG;
-  }
-  if (int e = check_method(b->method)) return e;
-  if (b->precision != RK_FP64 && b->precision != RK_FP32) {
-    set_error("rk_evolve: precision must be RK_FP64 or RK_FP32");
-    return RK_E_ARG;
-  }
-  if (b->nl_kind < RK_NL_NONE || b->nl_kind > RK_NL_NLS) {
-    set_error("rk_evolve: unknown nonlinearity kind");
-    return RK_E_ARG;
-  }
+  if (int e = validate_batch(b, true)) return e;
   if (b->n_inst <= 0) return RK_OK;
-  if (!b->n || !b->mode_off || !b->lin_op || !b->u || !b->state || !b->slab || !b->slab_off || !b->twiddle ||
-      !b->queue) {
-    set_error("rk_evolve: null device pointer");
-    return RK_E_ARG;
-  }
-  if (b->nl_kind == RK_NL_UUX && !b->kx) {
-    set_error("rk_evolve: RK_NL_UUX needs kx");
-    return RK_E_ARG;
-  }
   const int nmax = b->n_max;
-  const int limit = b->precision == RK_FP64 ? 4096 : 8192;
-  if (nmax < 4 || (nmax & (nmax - 1)) || nmax > limit) {
-    set_error("rk_evolve: n_max must be a power of two in [4, " + std::to_string(limit) + "]");
-    return RK_E_SIZE;
-  }
-  if (b->store_freq > 0 && (b->snap_cap <= 0 || !b->snap_u || !b->snap_t)) {
-    set_error("rk_evolve: snapshots requested without a snapshot buffer");
-    return RK_E_ARG;
-  }
-  if (b->etd.contour_points < 2) {
-    set_error("rk_evolve: contour_points must be > 1");
-    return RK_E_ARG;
-  }
-  if (b->threads != 0 && b->threads != 32 && b->threads != 64 && b->threads != 128 && b->threads != 256) {
-    set_error("rk_evolve: threads must be 0 (auto), 32, 64, 128 or 256");
-    return RK_E_ARG;
-  }
-  if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_ALL) {
-    set_error("rk_evolve: unknown placement");
-    return RK_E_ARG;
-  }
   cudaStream_t s = (cudaStream_t)stream;
   if (b->n_classes <= 0) {
     const int thr = b->threads > 0 ? b->threads : auto_threads(nmax);

@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     }
     if (!ok) flags[1] = 1;
     if (own) {
-      if (!ok) so.status = RK_E_CUDA;
+      if (!ok) so.status = RK_ST_WAIT_TIMEOUT;
       p.st[col0 + tid] = so;
     }
     if (have_state && !stop0) {

@@ -754,7 +754,7 @@ enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
-                         unsigned char* sm_slab, const cx<T>* tws, float* mlp_s) {
+                         unsigned char* sm_slab, const cx<T>* tws, float* mlp_s, int nfft) {
   using Tr = Traits<METHOD>;
   Ctx<T, CT, LOGN> x;
   x.g = g;
@@ -785,6 +785,17 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   rk_inst_state st = b.state[inst];
   // only RUNNING instances step; finished or failed ones keep their record untouched
   if (st.status != RK_ST_RUNNING) return;
+  {
+    // the shared-memory transforms (and the noalloc slabs) are sized for nfft points: an
+    // instance of another size is refused rather than stepped out of bounds
+    const int ni = b.n[inst];
+    const bool bad = LOGN > 0 ? (ni != (1 << LOGN)) : (ni < 4 || (ni & (ni - 1)) != 0 || ni > nfft);
+    if (bad) {
+      if (g.tid == 0) b.state[inst].status = RK_ST_BAD_SIZE;
+      g.sync();
+      return;
+    }
+  }
   cx<T>* uio = reinterpret_cast<cx<T>*>(b.u) + mo;
   for (int j = g.tid; j < x.m; j += g.nthr) x.u[j] = uio[j];
   g.sync();
@@ -995,7 +1006,7 @@ __global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const 
     g.sync();
     if (item >= count) break;
     const int inst = order ? order[item] : item;
-    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s);
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s, nfft);
   }
 }
 

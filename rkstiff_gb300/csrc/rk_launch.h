@@ -11,6 +11,9 @@ namespace rk {
 void set_error(const std::string& msg);
 int cuda_check(cudaError_t e, const char* what);
 
+// rk_evolve's argument checks (rk_api.cu); need_scratch = false skips slab, slab_off, queue
+int validate_batch(const rk_batch* b, bool need_scratch);
+
 // One launch of the evolve kernel over `count` items of `order`, all of grid size n
 // (n = 0: mixed sizes up to b.n_max, runtime-size kernel).
 struct ClassLaunch {

@@ -21,8 +21,33 @@ namespace rk {
 // scratch shared by every call: [64 queue counters | slab offsets | slabs]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[RK_NOALLOC_SCRATCH_BYTES];
 
+// Device address of g_noalloc_scratch per device, with the context it was looked up in.
+// The host-side symbol is only a stand-in: a kernel handed it would fault or, where the
+// GPU can reach host memory, use the wrong memory.
+struct NoallocSlot {
+  void* ctx;
+  void* ptr;
+};
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[64];  // device address of g_noalloc_scratch, per device
+static NoallocSlot g_noalloc_slot[64];
+
+typedef int (*ctx_get_current_fn)(void**);
+
+// cuCtxGetCurrent from the driver (through the runtime's entry-point query, so the library
+// needs no link against libcuda); NULL when the driver does not offer it
+static ctx_get_current_fn ctx_get_current() {
+  static ctx_get_current_fn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<ctx_get_current_fn>(p);
+  }
+  return fn;
+}
 
 // Offsets of instance i's slab: a uniform stride (the slab of the largest grid), so no
 // per-instance sizes are read back from the device.  Also invalidates each instance's
@@ -39,29 +64,22 @@ __global__ void noalloc_prepare_kernel(int64_t* slab_off, int64_t n_inst, int64_
 using namespace rk;
 
 extern "C" int rk_evolve_noalloc(const rk_batch* b, void* stream) {
-  if (!b || !b->state || b->n_inst < 0) {
-    set_error("rk_evolve_noalloc: invalid batch");
-    return RK_E_ARG;
-  }
+  // every argument check of rk_evolve runs before anything is launched, so a rejected call
+  // leaves the caller's state records untouched
+  if (int e = validate_batch(b, false)) return e;
   if (b->n_inst == 0) return RK_OK;
-  if (b->method < RK_IF34 || b->method > RK_IF4 || (b->precision != RK_FP64 && b->precision != RK_FP32)) {
-    set_error("rk_evolve_noalloc: unknown method or precision");
-    return RK_E_ARG;
-  }
-  if (b->n_max < 4 || (b->n_max & (b->n_max - 1))) {
-    set_error("rk_evolve_noalloc: n_max must be a power of two >= 4");
-    return RK_E_SIZE;
-  }
   const int64_t m_max = (b->nl_kind == RK_NL_UUX) ? b->n_max / 2 + 1 : b->n_max;
   const int64_t stride = (slab_bytes(b->method, b->precision, b->coef_complex, m_max) + 255) / 256 * 256;
-  const int64_t off_bytes = (b->n_inst * (int64_t)sizeof(int64_t) + 255) / 256 * 256;
-  const int64_t need = 256 + off_bytes + b->n_inst * stride;
-  if (need > (int64_t)RK_NOALLOC_SCRATCH_BYTES) {
-    set_error("rk_evolve_noalloc: the batch needs " + std::to_string(need) + " bytes of scratch, more than the " +
-              std::to_string((long long)RK_NOALLOC_SCRATCH_BYTES) +
-              " bytes this entry point holds; use rk_evolve with caller-allocated scratch");
+  // bound the instance count before any product: 256 bytes of counters, 8 bytes of offset
+  // and one slab per instance, plus at most 255 bytes of offset-table padding
+  const int64_t avail = (int64_t)RK_NOALLOC_SCRATCH_BYTES - 256 - 255;
+  if (b->n_inst > avail / (stride + (int64_t)sizeof(int64_t))) {
+    set_error("rk_evolve_noalloc: " + std::to_string((long long)b->n_inst) + " instances of n_max " +
+              std::to_string(b->n_max) + " need more than the " + std::to_string((long long)RK_NOALLOC_SCRATCH_BYTES) +
+              " bytes of scratch this entry point holds; use rk_evolve with caller-allocated scratch");
     return RK_E_SIZE;
   }
+  const int64_t off_bytes = (b->n_inst * (int64_t)sizeof(int64_t) + 255) / 256 * 256;
   int dev = 0;
   if (int e = cuda_check(cudaGetDevice(&dev), "cudaGetDevice")) return e;
   if (dev < 0 || dev >= 64) {
@@ -70,15 +88,21 @@ extern "C" int rk_evolve_noalloc(const rk_batch* b, void* stream) {
   }
   void* base = nullptr;
   {
-    // set-up, once per device, with that device current: the device address of the
-    // scratch array (the host-side symbol is only a stand-in and must not reach a kernel)
+    // set-up, once per device (and again only if that device's context was replaced, e.g.
+    // after cudaDeviceReset), with the device current: the array's device address
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    void* ctx = nullptr;
+    if (ctx_get_current_fn f = ctx_get_current()) {
+      if (f(&ctx) != 0) ctx = nullptr;
+    }
+    NoallocSlot& sl = g_noalloc_slot[dev];
+    if (!sl.ptr || sl.ctx != ctx) {
       void* p = nullptr;
       if (int e = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")) return e;
-      g_noalloc_ptr[dev] = p;
+      sl.ptr = p;
+      sl.ctx = ctx;
     }
-    base = g_noalloc_ptr[dev];
+    base = sl.ptr;
   }
   unsigned char* sc = static_cast<unsigned char*>(base);
   rk_batch b2 = *b;

@@ -176,7 +176,7 @@ class DenseEnsemble:
                 b.max_attempts = int(max_attempts)
                 nat.check(self.lib.rk_dense_evolve(ctypes.byref(b), stream.cuda_stream), "rk_dense_evolve")
         self.state = self.get_state()
-        if per_instance and np.any(self.state["status"] == nat.RK_E_CUDA):
+        if per_instance and np.any(self.state["status"] == nat.RK_ST_WAIT_TIMEOUT):
             raise nat.NativeError("rk_dense_eig_evolve: a device wait timed out")
         return self.state
 

@@ -20,7 +20,7 @@ from .models import BuiltinNL
 
 STATUS_NAMES = {nat.RK_ST_DONE: "done", nat.RK_ST_MAX_LOOPS: "max_loops", nat.RK_ST_MIN_STEP: "min_step",
                 nat.RK_ST_RUNNING: "running", nat.RK_ST_ITER_CAP: "iter_cap", nat.RK_ST_SNAP_FULL: "snap_full",
-                nat.RK_ST_STEP_DONE: "step_done"}
+                nat.RK_ST_STEP_DONE: "step_done", nat.RK_ST_BAD_SIZE: "bad_size"}
 
 
 class Ensemble:

@@ -42,8 +42,11 @@ def construct_x_cheb(n: int, a: float = -1.0, b: float = 1.0) -> np.ndarray:
 
 
 def construct_x_dx_cheb(n: int, a: float = -1, b: float = 1) -> Tuple[np.ndarray, np.ndarray]:
-    """Chebyshev points and the (n+1) x (n+1) first-derivative matrix (negative-sum trick
-    on the diagonal)."""
+    """Chebyshev points and the (n+1) x (n+1) first-derivative matrix: the published
+    construction of L. N. Trefethen, Spectral Methods in MATLAB (SIAM, 2000), program
+    cheb.m -- off-diagonal entries c_i/c_j (-1)^(i+j) / (x_i - x_j) with c = 2 at the ends,
+    the diagonal by the negative-sum trick (each row sums to zero).  The same matrix as the
+    reference's construct_x_dx_cheb (rkstiff/grids.py:178-219)."""
     x = construct_x_cheb(n, a, b)
     c = np.r_[2, np.ones(n - 1), 2] * np.power(-1, np.arange(0, n + 1))
     X = np.tile(x.reshape(n + 1, 1), (1, n + 1))

@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is available:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the rkstiff source tree> [case ...]
 
 The reference package is copied to a scratch directory (its ``__init__`` imports a
 setuptools-scm generated ``__version__`` module, which the copy supplies) and imported
@@ -386,7 +386,9 @@ CASES = (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases), ("adaptive",
 
 def main():
     """make_golden.py [reference root] [case names...]: every case file by default."""
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the rkstiff source tree> [case ...]")
+    ref_root = sys.argv[1]
     only = set(sys.argv[2:])
     tmp = import_reference(ref_root)
     try:

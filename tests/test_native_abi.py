@@ -137,3 +137,42 @@ def test_dense_eig_struct_layout_matches_c():
     assert vals[0] == ctypes.sizeof(nat.RkDenseEigBatch)
     for f, o in zip(fields, vals[1:]):
         assert getattr(nat.RkDenseEigBatch, f).offset == o, f
+
+
+def _fake_batch(n_inst, n_max):
+    """A batch whose device pointers are placeholders: only calls that the host-side checks
+    reject may be made with it (nothing dereferences them before those checks)."""
+    b = nat.RkBatch()
+    b.method = nat.RK_ETD35
+    b.precision = nat.RK_FP64
+    b.nl_kind = nat.RK_NL_UUX
+    b.n_inst = n_inst
+    b.n_max = n_max
+    for f in ("n", "mode_off", "lin_op", "kx", "u", "state", "twiddle"):
+        setattr(b, f, 0x1000)
+    b.etd = nat.RkEtdConfig(modecutoff=0.01, contour_radius=1.0, contour_points=32, reserved=0)
+    return b
+
+
+def test_noalloc_size_check_cannot_overflow(lib):
+    """rk_evolve_noalloc bounds the instance count before it multiplies by the slab stride:
+    counts whose products wrap int64 are refused, as are counts just past the scratch size.
+    Run only where no GPU is present, so that the placeholder pointers can never reach a
+    kernel."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("placeholder-pointer checks run on hosts without a GPU")
+    stride = (lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP64, 0, 2049) + 255) // 256 * 256
+    fits = (8 * 2**20 - 511) // (stride + 8)
+    for n_inst in (2**63 - 1, 2**63 // stride + 1, (2**64 // stride) // 2, fits + 1, 10**6):
+        rc = lib.rk_evolve_noalloc(ctypes.byref(_fake_batch(n_inst, 4096)), None)
+        assert rc == nat.RK_E_SIZE, n_inst
+        assert b"scratch" in lib.rk_last_error()
+    # argument errors are found before the size check, as in rk_evolve
+    b = _fake_batch(2, 4096)
+    b.kx = None
+    assert lib.rk_evolve_noalloc(ctypes.byref(b), None) == nat.RK_E_ARG
+    b = _fake_batch(2, 3000)
+    assert lib.rk_evolve_noalloc(ctypes.byref(b), None) == nat.RK_E_SIZE
+    assert b"power of two" in lib.rk_last_error()
