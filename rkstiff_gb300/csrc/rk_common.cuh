@@ -63,6 +63,11 @@ RK_DEV cx<double> cexp(cx<double> z) {
 }
 
 template <class T> RK_DEV cx<T> ld(const cx<T>* p, int64_t i) { return p[i]; }
+template <class T> RK_DEV void cx_ptr_swap(cx<T>*& a, cx<T>*& b) {
+  cx<T>* t = a;
+  a = b;
+  b = t;
+}
 
 // ---------------------------------------------------------------------------------
 // Thread groups: `nthr` consecutive threads (a multiple of 32) that own one instance.

@@ -39,13 +39,24 @@ RK_HD int traits_nn(int method) {
   return 0;
 }
 
-// bytes of an instance's scratch: u, unew, N1..NN (complex T) and the coefficient block
+// ETD35 / ETD5 write the new state into N2's array: neither the new state nor the error
+// combination reads N2 (etd35.py:337-344, etd5.py:248-252; a72 = 0), so the method needs one
+// state vector fewer -- 7 complex vectors u, N1..N6 instead of 8
+RK_HD constexpr bool unew_in_n2(int method) { return method == RK_ETD35 || method == RK_ETD5; }
+
+// complex vectors of an instance's scratch
+RK_HD int traits_nv(int method) { return traits_nn(method) + (unew_in_n2(method) ? 1 : 2); }
+
+// bytes of an instance's scratch: u, unew, N1..NN (complex T), the coefficient block and,
+// in FP32, a working-precision copy of the wavenumbers (read once per nonlinear evaluation
+// per mode; converting the FP64 input there would put a conversion per mode on the FP64 pipe)
 RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m) {
   const int64_t mp = round_up4(m);
   const int64_t ts = precision == RK_FP64 ? 8 : 4;
   const int64_t vec = 2 * ts * mp;
   const int64_t coef = (coef_complex ? 2 : 1) * ts * mp;
-  return (2 + traits_nn(method)) * vec + num_coeffs(method) * coef;
+  const int64_t kxw = precision == RK_FP64 ? 0 : ts * mp;
+  return traits_nv(method) * vec + num_coeffs(method) * coef + kxw;
 }
 
 // ---------------------------------------------------------------------------------
@@ -58,7 +69,7 @@ struct Ctx {
   Group g;
   int n, logn, m, mp, nl_kind;
   T nl_c;
-  const double* kx;
+  const T* kx;  // wavenumbers in the working precision (u*ux only)
   const cx<double>* lin;
   cx<T>* u;
   cx<T>* unew;
@@ -147,7 +158,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
         const int j = j0 + q * g.nthr;
         const bool in = j <= M;
         kv[q] = in ? kf(j) : cx<T>{T(0), T(0)};
-        kxv[q] = in ? T(x.kx[j]) : T(0);
+        kxv[q] = in ? x.kx[j] : T(0);
       }
 #pragma unroll
       for (int q = 0; q < PK; ++q) {
@@ -752,6 +763,14 @@ RK_DEV float safe_log(double v) { return (v > 0.0 && v < 1e300) ? (float)log(v) 
 // ---------------------------------------------------------------------------------
 enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 
+// u <- unew after an accepted step.  With the new state in N2's array the two arrays swap
+// roles: the old u array becomes N2 (and the next new state's home).
+template <bool U2, class X>
+RK_DEV void accept_swap(X& x) {
+  cx_ptr_swap(x.u, U2 ? x.N[1] : x.unew);
+  if (U2) x.unew = x.N[1];
+}
+
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
                          unsigned char* sm_slab, const cx<T>* tws, float* mlp_s, int nfft) {
@@ -765,15 +784,15 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.mp = (int)round_up4(x.m);
   x.nl_c = T(b.nl_coef);
   const int64_t mo = b.mode_off[inst];
-  x.kx = b.kx ? b.kx + mo : nullptr;
   x.lin = reinterpret_cast<const cx<double>*>(b.lin_op) + mo;
   cx<T>* gsl = reinterpret_cast<cx<T>*>(reinterpret_cast<char*>(b.slab) + b.slab_off[inst]);
   cx<T>* ssl = PLACE == PL_GLOBAL ? gsl : reinterpret_cast<cx<T>*>(sm_slab);
+  constexpr bool U2 = unew_in_n2(METHOD);
+  constexpr int NV = Tr::NN + (U2 ? 1 : 2);  // complex vectors before the coefficient block
   x.u = ssl;
-  x.unew = ssl + x.mp;
-  for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + (2 + i) * x.mp : nullptr;
-  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + (2 + Tr::NN) * x.mp)
-                             : reinterpret_cast<CT*>(gsl + (2 + Tr::NN) * x.mp);
+  for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + ((U2 ? 1 : 2) + i) * x.mp : nullptr;
+  x.unew = U2 ? x.N[1] : ssl + x.mp;
+  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NV * x.mp) : reinterpret_cast<CT*>(gsl + NV * x.mp);
   x.fa = fa;
   x.fb = fb;
   x.red = red;
@@ -794,6 +813,21 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       if (g.tid == 0) b.state[inst].status = RK_ST_BAD_SIZE;
       g.sync();
       return;
+    }
+  }
+  x.kx = nullptr;
+  if (b.kx) {
+    if constexpr (sizeof(T) == sizeof(double)) {
+      x.kx = b.kx + mo;
+    } else {
+      // FP32: a working-precision copy after the coefficient block (shared memory when the
+      // stage arrays are there, the global slab otherwise), filled once per launch
+      T* kw = PLACE == PL_GLOBAL ? reinterpret_cast<T*>(reinterpret_cast<CT*>(gsl + NV * x.mp) + Tr::NC * x.mp)
+            : PLACE == PL_SMEM_STATE ? reinterpret_cast<T*>(ssl + NV * x.mp)
+                                     : reinterpret_cast<T*>(x.C + Tr::NC * x.mp);
+      const double* kd = b.kx + mo;
+      for (int j = g.tid; j < x.m; j += g.nthr) kw[j] = T(kd[j]);
+      x.kx = kw;
     }
   }
   cx<T>* uio = reinterpret_cast<cx<T>*>(b.u) + mo;
@@ -856,7 +890,9 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
           }
         }
         ++attempts;
-        const float f_s = clampf(safe_log(s), -8.f, 8.f);
+        // log s feeds only the learned controller's features (an FP64 log per attempt
+        // would otherwise hold the slow FP64 pipe)
+        const float f_s = learned ? clampf(safe_log(s), -8.f, 8.f) : 0.f;
         if (!ok) {
           accept = false;
           ++rejects;
@@ -905,7 +941,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       }
       if (status != RK_ST_RUNNING) break;
       // accepted: u <- unew; FSAL methods carry N(unew) into N1
-      { cx<T>* tmp = x.u; x.u = x.unew; x.unew = tmp; }
+      accept_swap<U2>(x);
       if (Tr::FSAL) { cx<T>* tmp = x.N[0]; x.N[0] = x.N[Tr::NN - 1]; x.N[Tr::NN - 1] = tmp; }
       t += h;
       h_used = h;
@@ -930,7 +966,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       run_attempt<T, CT, METHOD>(x, h, ctl, nlc);
       nl_evals += nlc;
       ++attempts;
-      { cx<T>* tmp = x.u; x.u = x.unew; x.unew = tmp; }
+      accept_swap<U2>(x);
       t += h;
       h_used = h;
     }
@@ -1028,8 +1064,9 @@ template <class T, class CT, int METHOD>
 inline size_t smem_slab_bytes(int place, int64_t m) {
   const size_t mp = (size_t)round_up4(m);
   size_t bytes = 0;
-  if (place >= PL_SMEM_STATE) bytes += (2 + Traits<METHOD>::NN) * mp * sizeof(cx<T>);
+  if (place >= PL_SMEM_STATE) bytes += (size_t)traits_nv(METHOD) * mp * sizeof(cx<T>);
   if (place >= PL_SMEM_ALL) bytes += Traits<METHOD>::NC * mp * sizeof(CT);
+  if (place >= PL_SMEM_STATE && sizeof(T) == sizeof(float)) bytes += mp * sizeof(T);  // wavenumbers
   return bytes;
 }
 

@@ -183,16 +183,23 @@ RK_DEV void dft_reg(cx<T>* v) {
   }
 }
 
-// radix of pass p for a size-2^LOGN transform: 16 while >= 4 bits remain... then the rest
+// radix of pass p for a size-2^LOGN transform: 16 while >= 4 bits remain, then the rest,
+// preferring 8+8 over 16+4 / 16+2 splits of the last 6/5 bits; the radix is capped so that
+// a pass has at least 32 butterflies (N / R >= 32), which keeps every lane of a one-warp
+// group busy on the small transforms (n = 128, 256) instead of half or a quarter of them.
 template <int LOGN, int P>
 struct PassRadix {
+  __host__ __device__ static constexpr int pick(int left) {
+    int lg = left >= 4 ? 4 : left;
+    if (left == 6 || left == 5) lg = 3;
+    if (left == 7) lg = 4;
+    const int cap = LOGN - 5 < 1 ? 1 : LOGN - 5;
+    return lg > cap ? cap : lg;
+  }
   __host__ __device__ static constexpr int used() {
     int left = LOGN, lg = 0;
     for (int q = 0; q <= P; ++q) {
-      lg = left >= 4 ? 4 : left;
-      // prefer 8+8 over 16+4 / 16+2 splits of the last 6/5 bits
-      if (left == 6 || left == 5) lg = 3;
-      if (left == 7) lg = 4;
+      lg = pick(left);
       left -= lg;
     }
     return lg;
@@ -200,9 +207,7 @@ struct PassRadix {
   __host__ __device__ static constexpr int bits_before() {
     int left = LOGN, done = 0;
     for (int q = 0; q < P; ++q) {
-      int lg = left >= 4 ? 4 : left;
-      if (left == 6 || left == 5) lg = 3;
-      if (left == 7) lg = 4;
+      const int lg = pick(left);
       left -= lg;
       done += lg;
     }

@@ -311,6 +311,59 @@ def failure_cases(out):
             out["fail_burg"] = np.array(2)
         except BaseSolverAS.MaxLoopsExceeded:
             out["fail_burg"] = np.array(1)
+        # a non-finite state: every attempt's s is NaN, h shrinks by 0.25 per rejection, and
+        # with minh = 1e-300 the retry bound (more than 50 loops) is met first
+        x, kx, lin, nl = ks_problem(64, 22.0)
+        u0 = np.fft.rfft(np.cos(2 * np.pi * x / 22.0))
+        u0[3] = np.nan
+        s = etd35.ETD35(lin, nl, config=SolverConfig(minh=1e-300))
+        rec = Recorder(s)
+        try:
+            s.evolve(u0, t0=0.0, tf=1.0, h_init=0.1, store_data=False)
+            out["fail_nan"] = np.array(0)
+        except BaseSolverAS.MaxLoopsExceeded:
+            out["fail_nan"] = np.array(1)
+        except BaseSolverAS.MinimumStepReached:
+            out["fail_nan"] = np.array(2)
+        out["fail_nan_attempts"] = np.array(len(rec.s))
+
+
+def nls_solitons_u0(n, seed):
+    """Three seeded solitons on [-50, 50): A_j sech(A_j (x - x_j)) exp(i v_j x) with
+    A_j ~ U[0.5, 2], x_j ~ U[-30, 30], v_j ~ U[-1, 1] (the draw order of
+    rkstiff_gb300.workloads.nls_solitons)."""
+    rng = np.random.default_rng(seed)
+    x = -50.0 + np.arange(n) * (100.0 / n)
+    A = rng.uniform(0.5, 2.0, 3)
+    x0 = rng.uniform(-30.0, 30.0, 3)
+    v = rng.uniform(-1.0, 1.0, 3)
+    return np.fft.fft(sum(A[j] / np.cosh(A[j] * (x - x0[j])) * np.exp(1j * v[j] * x) for j in range(3)))
+
+
+def nls4096_cases(out):
+    """The NLS soliton configuration at its full size: n = 4096 on [-50, 50), ETD35,
+    epsilon = 1e-6, t in [0, 20], snapshots every 50 accepted steps."""
+    from rkstiff import etd35
+    from rkstiff.solveras import SolverConfig
+    x, kx, lin, nl = nls_problem(4096, -50.0, 50.0)
+    u0 = nls_solitons_u0(4096, 0)
+    calls = [0]
+
+    def counted(u):
+        calls[0] += 1
+        return nl(u)
+    s = etd35.ETD35(lin, counted, config=SolverConfig(epsilon=1e-6))
+    rec = Recorder(s)
+    out["nls4096_u0"] = u0
+    out["nls4096_ETD35_final"] = s.evolve(u0, t0=0.0, tf=20.0, store_freq=50)
+    out["nls4096_ETD35_t"] = np.array(s.t)
+    out["nls4096_ETD35_s"] = np.array(rec.s)
+    out["nls4096_ETD35_nl_calls"] = np.array(calls[0])
+    # one step of the same problem from u0 at h = 0.02 (the one-step gate of FP32 runs)
+    s1 = etd35.ETD35(lin, nl, config=SolverConfig(epsilon=1e-6))
+    u1, h1, hs1 = s1.step(u0, 0.02)
+    out["nls4096_step_u"] = u1
+    out["nls4096_step_h"] = np.array([h1, hs1])
 
 
 def multid_cases(out):
@@ -381,7 +434,7 @@ def multid_cases(out):
 
 CASES = (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases), ("adaptive", adaptive_cases),
          ("controller", controller_cases), ("dense", dense_cases), ("failure", failure_cases),
-         ("multid", multid_cases))
+         ("multid", multid_cases), ("nls4096", nls4096_cases))
 
 
 def main():

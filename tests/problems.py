@@ -87,3 +87,9 @@ def allen_cahn(n, eps=0.01):
     def nl(u):
         return np.asarray(xi - np.power(u + xi, 3), dtype=np.complex128).ravel()
     return x, lin, nl
+
+
+def nls4096():
+    """The NLS soliton configuration's grid and operator: n = 4096 on [-50, 50)."""
+    x, kx = fft_grid(4096, -50.0, 50.0)
+    return kx, -0.5j * kx**2, nls_nl

@@ -42,8 +42,8 @@ def test_abi_version_and_sizes(lib):
     assert lib.rk_num_coeffs(nat.RK_IF34) == 2
     assert lib.rk_num_coeffs(nat.RK_IF45DP) == 28
     assert lib.rk_num_coeffs(99) < 0
-    # ETD35, FP32, real coefficients, m=513 -> mp=516: 8 complex arrays + 21 real arrays
-    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 0, 513) == 8 * 8 * 516 + 21 * 4 * 516
+    # ETD35, FP32, real coefficients, m=513 -> mp=516: 7 complex arrays (the new state shares N2's) + 21 real arrays + wavenumbers
+    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 0, 513) == 7 * 8 * 516 + 21 * 4 * 516 + 4 * 516
     assert lib.rk_slab_bytes(nat.RK_IF34, nat.RK_FP64, 1, 100) == 7 * 16 * 100 + 2 * 16 * 100
     assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP64, 0, 0) < 0
 

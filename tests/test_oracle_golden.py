@@ -257,3 +257,32 @@ def test_dense_coeffs_eig_vs_reference_contour_arrays(golden):
     for name in ("a21", "a54", "a65", "a76"):
         assert _close(C[name], g[f"ac20_ETD35_dense_{name}"], 3e-5), name
     assert _close(C["E"], g["ac20_ETD35_dense_EL"], 1e-13)
+
+
+def test_failure_nan_state_max_loops(golden):
+    """A non-finite state with minh = 1e-300: the reference raises MaxLoopsExceeded after 51
+    attempts (more than 50 retries, solveras.py:399-406); the oracle does the same."""
+    g = golden("failure")
+    assert int(g["fail_nan"]) == 1 and int(g["fail_nan_attempts"]) == 51
+    x, kx, lin, nl = P.ks(64, 22.0)
+    u0 = np.fft.rfft(np.cos(2 * np.pi * x / 22.0))
+    u0[3] = np.nan
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(minh=1e-300))
+    with pytest.raises(O.MaxLoopsExceeded):
+        s.evolve(u0, 0.0, 1.0, h_init=0.1, store_data=False)
+    assert s.attempts == 51
+
+
+def test_adaptive_nls4096_etd35(golden):
+    """The NLS soliton configuration at full size (n = 4096, eps = 1e-6, t in [0, 20])."""
+    g = golden("nls4096")
+    kx, lin, nl = P.nls4096()
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-6))
+    uf = s.evolve(g["nls4096_u0"], 0.0, 20.0, store_freq=50)
+    np.testing.assert_allclose([r[2] for r in s.log], g["nls4096_ETD35_s"], rtol=1e-9)
+    np.testing.assert_allclose(s.t, g["nls4096_ETD35_t"], rtol=1e-13)
+    assert _close(uf, g["nls4096_ETD35_final"], 1e-11)
+    o = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-6))
+    u1, h1, hs1 = o.step(g["nls4096_u0"], 0.02)
+    assert [h1, hs1] == pytest.approx(list(g["nls4096_step_h"]), rel=1e-12)
+    assert _close(u1, g["nls4096_step_u"], 1e-13)
