@@ -385,6 +385,35 @@ int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream);
 int64_t rk_tf32x3_work_bytes(int64_t K, int64_t N);
 int rk_tf32x3_gemm(const float* A, const float* B, float* D, int64_t K, int64_t N, void* work, void* stream);
 
+/* Device grids and spectral derivatives (set-up helpers, so that a problem's operators and
+ * initial data can be built without leaving the GPU).  FP64, all arrays [device].
+ *   rk_fourier_grid: x[n] = a + j*delta, delta = (a + dx) - a, and kx = 2 pi k / (n dx) with
+ *       k the rfft (real_grid = 1, n/2 + 1 entries) or fft (n entries) frequency integers:
+ *       construct_x_kx_rfft / construct_x_kx_fft, rkstiff/grids.py:40-85 / 88-131 (the
+ *       caller passes dx = (b - a)/n, as the reference computes it); bitwise NumPy's values.
+ *       Either output may be NULL.
+ *   rk_cheb_grid: the n + 1 Chebyshev extreme points on [a, b] and (D not NULL) the
+ *       (n+1) x (n+1) row-major first-derivative matrix: construct_x_cheb /
+ *       construct_x_dx_cheb, rkstiff/grids.py:134-219.
+ *   rk_dx_fourier: `rows` rows of n points (2 <= n <= 4096; powers of two by FFT, other
+ *       n by direct DFT over the n roots of unity): the order-th
+ *       derivative irfft((i kx)^order rfft(u)) of real rows (real_grid = 1, u and out
+ *       float64, kx n/2 + 1 entries; dx_rfft, rkstiff/derivatives.py:47-124) or
+ *       ifft((i kx)^order fft(u)) of complex rows (real_grid = 0, complex128, kx n entries;
+ *       dx_fft, rkstiff/derivatives.py:126-180).  twiddle64: the RK_TW_N FP64 table of
+ *       rk_fill_twiddles.
+ *   rk_dx_cheb: out = D^order u, D n x n, u n x cols (row-major, cols = 1 for a vector):
+ *       dx_cheb, rkstiff/derivatives.py:182-253 (D^order formed first by repeated products,
+ *       as numpy.linalg.matrix_power; work holds rk_dx_cheb_work_bytes(n) bytes when
+ *       order > 1). */
+int rk_fourier_grid(int32_t real_grid, int64_t n, double a, double dx, double* x, double* kx, void* stream);
+int rk_cheb_grid(int64_t n, double a, double b, double* x, double* D, void* stream);
+int rk_dx_fourier(int32_t real_grid, int32_t order, int64_t n, int64_t rows, const double* kx, const void* u,
+                  void* out, const void* twiddle64, void* stream);
+int64_t rk_dx_cheb_work_bytes(int64_t n);
+int rk_dx_cheb(int32_t order, int64_t n, int64_t cols, const double* D, const double* u, double* out, void* work,
+               void* stream);
+
 /* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
  * each run 8 independent FP32 FMA chains of `iters` steps and write one float to
  * out[blocks*threads] [device].  FLOPs = 16 * blocks * threads * iters; timing it gives the

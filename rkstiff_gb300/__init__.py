@@ -10,7 +10,7 @@ stiff PDEs u_t = L u + N(u)) as GB300 (sm_103a) CUDA kernels behind rkstiff's so
 The native library is built in-tree on first use (``rkstiff_gb300._build.build()``).
 """
 
-from . import grids, models, transforms  # noqa: F401
+from . import derivatives, grids, models, transforms  # noqa: F401
 from .device import DeviceOptions  # noqa: F401
 from .etd import ETDAS, ETDCS, ETDConfig, psi1, psi2, psi3  # noqa: F401
 from .etd34 import ETD34  # noqa: F401

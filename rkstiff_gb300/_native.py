@@ -109,7 +109,8 @@ assert STATE_DTYPE.itemsize == 128
 EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
-           "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve")
+           "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve",
+           "rk_fourier_grid", "rk_cheb_grid", "rk_dx_fourier", "rk_dx_cheb_work_bytes", "rk_dx_cheb")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -175,6 +176,14 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_error_s.restype = ctypes.c_int
         lib.rk_cgemv.argtypes = [i32, i64, vp, vp, vp, vp]
         lib.rk_cgemv.restype = ctypes.c_int
+        lib.rk_fourier_grid.argtypes = [i32, i64, dbl, dbl, vp, vp, vp]
+        lib.rk_cheb_grid.argtypes = [i64, dbl, dbl, vp, vp, vp]
+        lib.rk_dx_fourier.argtypes = [i32, i32, i64, i64, vp, vp, vp, vp, vp]
+        lib.rk_dx_cheb_work_bytes.argtypes = [i64]
+        lib.rk_dx_cheb_work_bytes.restype = i64
+        lib.rk_dx_cheb.argtypes = [i32, i64, i64, vp, vp, vp, vp, vp]
+        for fn in (lib.rk_fourier_grid, lib.rk_cheb_grid, lib.rk_dx_fourier, lib.rk_dx_cheb):
+            fn.restype = ctypes.c_int
         if lib.rk_abi_version() != 1:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

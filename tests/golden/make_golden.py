@@ -366,6 +366,62 @@ def nls4096_cases(out):
     out["nls4096_step_h"] = np.array([h1, hs1])
 
 
+def derivs_cases(out):
+    """Grids and spectral derivatives of rkstiff/grids.py and rkstiff/derivatives.py on the
+    inputs of the reference's own tests plus larger seeded ones."""
+    from rkstiff import grids, derivatives
+    for tag, (n, a, b) in {"g1024": (1024, 0.0, 32 * np.pi), "g4096": (4096, -50.0, 50.0), "g256": (256, -30.0, 30.0),
+                           "g100": (100, 0.0, 2 * np.pi), "g400": (400, -30.0, 30.0), "g8": (8, 0.0, 2 * np.pi)}.items():
+        x, kx = grids.construct_x_kx_rfft(n, a, b)
+        out[f"rfft_{tag}_x"], out[f"rfft_{tag}_kx"] = x, kx
+        out[f"fft_{tag}_kx"] = grids.construct_x_kx_fft(n, a, b)[1]
+    for tag, (n, a, b) in {"c20": (20, -1, 1), "c30": (30, -3, 3), "c128": (128, -1, 1)}.items():
+        x, D = grids.construct_x_dx_cheb(n, a, b)
+        out[f"cheb_{tag}_x"] = x
+        if n <= 30:
+            out[f"cheb_{tag}_D"] = D
+    # dx_rfft: tests/test_derivatives_rfft.py inputs (N = 8, 16) and seeded rows
+    for N, order in ((8, 1), (16, 2)):
+        L = 2 * np.pi
+        x = np.linspace(0, L, N, endpoint=False)
+        kx = np.fft.rfftfreq(N, d=L / N) * 2 * np.pi
+        out[f"drfft_{N}_{order}"] = derivatives.dx_rfft(kx, np.sin(x), n=order)
+    rng = np.random.default_rng(31)
+    for N in (1024, 100):
+        x, kx = grids.construct_x_kx_rfft(N, 0.0, 22.0)
+        u = rng.standard_normal(N) * np.exp(-np.abs(np.fft.fftfreq(N) * N) / 8)
+        out[f"drfft_rand{N}_u"] = u
+        for order in (1, 2, 3):
+            out[f"drfft_rand{N}_{order}"] = derivatives.dx_rfft(kx, u, n=order)
+    # dx_fft: tests/test_derivatives_fft.py inputs
+    x, kx = grids.construct_x_kx_fft(128, 0, 2 * np.pi)
+    v = np.sin(x)
+    for _ in range(4):
+        v = derivatives.dx_fft(kx, v)
+    out["dfft_many4"] = v
+    out["dfft_order8"] = derivatives.dx_fft(kx, np.sin(x), 8)
+    x, kx = grids.construct_x_kx_fft(100, 0, 2 * np.pi)
+    out["dfft_periodic100"] = derivatives.dx_fft(kx, np.sin(x))
+    x, kx = grids.construct_x_kx_fft(400, -30.0, 30.0)
+    out["dfft_sech400"] = derivatives.dx_fft(kx, 1.0 / np.cosh(x))
+    x, kx = grids.construct_x_kx_fft(128, -10, 10)
+    out["dfft_gauss128"] = derivatives.dx_fft(kx, np.exp(-(x**2)))
+    x, kx = grids.construct_x_kx_fft(4096, -50.0, 50.0)
+    uc = (rng.standard_normal(4096) + 1j * rng.standard_normal(4096)) * np.exp(-np.abs(x) / 10)
+    out["dfft_rand4096_2"] = derivatives.dx_fft(kx, uc, 2)
+    # dx_cheb: tests/test_derivatives_cheb.py inputs, higher orders and a 2-D u
+    for tag, (n, a, b) in {"c20": (20, -1, 1), "c30": (30, -3, 3)}.items():
+        x, D = grids.construct_x_dx_cheb(n, a, b)
+        u = np.exp(x) * np.sin(5 * x)
+        for order in (1, 2, 3):
+            out[f"dcheb_{tag}_{order}"] = derivatives.dx_cheb(D, u, n=order)
+    x, D = grids.construct_x_dx_cheb(20, -1, 1)
+    U = np.stack([np.sin(x), np.cos(2 * x), x**3], axis=1)
+    out["dcheb_c20_2d_2"] = derivatives.dx_cheb(D, U, n=2)
+    arr = np.linspace(-1, 1, 8)
+    out["dcheb_swapped"] = derivatives.dx_cheb(arr, np.eye(8))
+
+
 def multid_cases(out):
     """The multi-dimensional spectral problems of the reference's NLS demo (demos/nls.ipynb):
     the radial NLS on a Hankel grid, the (r, t) NLS with a Hankel transform in r and an FFT
@@ -434,7 +490,8 @@ def multid_cases(out):
 
 CASES = (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases), ("adaptive", adaptive_cases),
          ("controller", controller_cases), ("dense", dense_cases), ("failure", failure_cases),
-         ("multid", multid_cases), ("nls4096", nls4096_cases))
+         ("multid", multid_cases), ("nls4096", nls4096_cases),
+         ("derivs", derivs_cases))
 
 
 def main():

@@ -286,3 +286,36 @@ def test_adaptive_nls4096_etd35(golden):
     u1, h1, hs1 = o.step(g["nls4096_u0"], 0.02)
     assert [h1, hs1] == pytest.approx(list(g["nls4096_step_h"]), rel=1e-12)
     assert _close(u1, g["nls4096_step_u"], 1e-13)
+
+
+def test_grids_and_derivatives(golden):
+    """The oracle's grids and spectral derivatives against the reference's own outputs
+    (grids bitwise; derivatives to rounding)."""
+    from oracle import derivs as OD
+
+    g = golden("derivs")
+    specs = {"g1024": (1024, 0.0, 32 * np.pi), "g4096": (4096, -50.0, 50.0), "g256": (256, -30.0, 30.0),
+             "g100": (100, 0.0, 2 * np.pi), "g400": (400, -30.0, 30.0), "g8": (8, 0.0, 2 * np.pi)}
+    for tag, (n, a, b) in specs.items():
+        x, kx = OD.fourier_grid(n, a, b, True)
+        assert np.array_equal(x, g[f"rfft_{tag}_x"]) and np.array_equal(kx, g[f"rfft_{tag}_kx"]), tag
+        assert np.array_equal(OD.fourier_grid(n, a, b, False)[1], g[f"fft_{tag}_kx"]), tag
+    for tag, (n, a, b) in {"c20": (20, -1, 1), "c30": (30, -3, 3), "c128": (128, -1, 1)}.items():
+        x, D = OD.cheb_grid(n, a, b)
+        assert _close(x, g[f"cheb_{tag}_x"], 1e-15), tag
+        if f"cheb_{tag}_D" in g:
+            assert _close(D, g[f"cheb_{tag}_D"], 1e-13), tag
+    for N, order in ((8, 1), (16, 2)):
+        L = 2 * np.pi
+        x = np.linspace(0, L, N, endpoint=False)
+        kx = np.fft.rfftfreq(N, d=L / N) * 2 * np.pi
+        assert _close(OD.dx_rfft(kx, np.sin(x), order), g[f"drfft_{N}_{order}"], 1e-14)
+    for N in (1024, 100):
+        _, kx = OD.fourier_grid(N, 0.0, 22.0, True)
+        for order in (1, 2, 3):
+            assert _close(OD.dx_rfft(kx, g[f"drfft_rand{N}_u"], order), g[f"drfft_rand{N}_{order}"], 1e-13)
+    x, kx = OD.fourier_grid(128, 0, 2 * np.pi, False)
+    assert _close(OD.dx_fft(kx, np.sin(x), 8), g["dfft_order8"], 1e-12)
+    x, D = OD.cheb_grid(20, -1, 1)
+    U = np.stack([np.sin(x), np.cos(2 * x), x**3], axis=1)
+    assert _close(OD.dx_cheb(D, U, 2), g["dcheb_c20_2d_2"], 1e-11)
