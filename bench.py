@@ -83,12 +83,13 @@ def _cpu_instance(args):
 
     s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=WORKLOAD["epsilon"]))
     status = 0
+    uf = None
     try:
-        s.evolve(u0, 0.0, WORKLOAD["tf"], store_data=False)
+        uf = s.evolve(u0, 0.0, WORKLOAD["tf"], store_data=False)
     except (O.MinimumStepReached, O.MaxLoopsExceeded):
         status = 1
     steps = sum(1 for r in s.log if r[3])
-    return n // 2 + 1, steps, s.attempts, status
+    return n // 2 + 1, steps, s.attempts, status, uf
 
 
 def _cpu_dense_instance(args):
@@ -115,7 +116,7 @@ def cpu_measure(pool, sample):
     t0 = time.perf_counter()
     res = pool.map(_cpu_instance, sample, chunksize=1)
     wall = time.perf_counter() - t0
-    mode_steps = sum(m * s for m, s, _, _ in res)
+    mode_steps = sum(r[0] * r[1] for r in res)
     return mode_steps / wall, wall, res
 
 
@@ -229,10 +230,122 @@ def measure_fp32_peak(device) -> float:
 
 
 FORMS = {"workload": "burgers_ensemble_etd35", "instances": 2048, "n": 512, "nu_range": [1e-3, 1e-1],
-         "epsilon": 1e-5, "tf": 5.0, "seed": 7, "reference_epsilon": 1e-10, "reference_sample": 256}
+         "epsilon": 1e-5, "tf": 5.0, "seed": 7, "reference_epsilon": 1e-10, "reference_sample": 256,
+         "precision_check_h": 0.005}
+
+# accuracy of the headline (FP32) against the FP64 oracle on a sample: one adaptive step from
+# u0 (the <= 1e-6 gate), and trajectories to a short horizon; chaotic KS at tf = 100 is
+# reported, not gated (the reference's own eps = 1e-5 run differs from a tight one by 1e-4..4e-3)
+ACCURACY = {"per_size": 4, "h_step": 0.01, "t_short": 10.0, "gate_one_step": 1e-6}
 
 
-def forms_comparison(dev) -> dict:
+def _rel(a, b) -> float:
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _stats(v) -> dict:
+    v = np.asarray(v, dtype=np.float64)
+    if v.size == 0:
+        return {"count": 0}
+    return {"count": int(v.size), "median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)),
+            "max": float(np.max(v))}
+
+
+def headline_accuracy(dev, inst, gpu_finals=None, oracle_finals=None) -> dict:
+    """rel L2 of the FP32 ensemble against the FP64 oracle (the reference's algorithm):
+    ACCURACY['per_size'] instances of each grid size, one adaptive step from u0 at
+    h = ACCURACY['h_step'] and the trajectory to t = ACCURACY['t_short'] (same epsilon); and,
+    when given, the tf = 100 states of the CPU-baseline sample (reported, not gated)."""
+    from oracle import rk_oracle as O
+    from rkstiff_gb300 import _native as nat
+    from rkstiff_gb300 import models
+    from rkstiff_gb300.ensemble import Ensemble
+    from rkstiff_gb300.solveras import SolverConfig
+
+    idx = []
+    for n in WORKLOAD["n_choices"]:
+        idx += [i for i, r in enumerate(inst) if r[0] == n][:ACCURACY["per_size"]]
+    eps, h, T = WORKLOAD["epsilon"], ACCURACY["h_step"], ACCURACY["t_short"]
+    lins, nls, u0s = [], [], []
+    for i in idx:
+        n, L, u0 = inst[i]
+        kx, lin = ks_operator(n, L)
+        lins.append(lin)
+        nls.append(models.ks_ops(kx)[1])
+        u0s.append(u0)
+    ens = Ensemble("ETD35", lins, nls, config=SolverConfig(epsilon=eps), precision="fp32", device=dev)
+    eng = ens.engine
+    u = eng.pack_u(u0s)
+    eng.put_state(eng.fresh_state(0.0, np.inf, h))
+    eng.launch(u, nat.RK_RUN_STEP)
+    st = eng.get_state()
+    one = [x.cpu().numpy() for x in eng.unpack_u(u)]
+    fin = [x.cpu().numpy() for x in ens.evolve(u0s, 0.0, T)]
+    one_err, same_h, short_err = [], 0, []
+    for k in range(len(idx)):
+        o = O.OracleSolver("ETD35", lins[k], nls[k], O.SolverConfig(epsilon=eps))
+        un, hu, _ = o.step(u0s[k].astype(np.complex128), h)
+        if hu == float(st["h_used"][k]):
+            same_h += 1
+            one_err.append(_rel(one[k], un))
+        o = O.OracleSolver("ETD35", lins[k], nls[k], O.SolverConfig(epsilon=eps))
+        short_err.append(_rel(fin[k], o.evolve(u0s[k].astype(np.complex128), 0.0, T, store_data=False)))
+    out = {"reference": "FP64 NumPy oracle of the reference's ETD35 (same epsilon)",
+           "sample": f"{ACCURACY['per_size']} instances per grid size {WORKLOAD['n_choices']} of the workload",
+           "one_step": {**_stats(one_err), "h": h, "same_step_size": same_h,
+                        "gate": ACCURACY["gate_one_step"],
+                        "pass": bool(one_err) and max(one_err) <= ACCURACY["gate_one_step"]},
+           f"t{int(T)}": _stats(short_err)}
+    if gpu_finals is not None and oracle_finals:
+        errs = [_rel(gpu_finals[i], oracle_finals[i]) for i in sorted(oracle_finals) if i < len(gpu_finals)]
+        out["tf100_reported_not_gated"] = {**_stats(errs), "sample": "the CPU baseline's instances (oracle to tf=100)"}
+    return out
+
+
+def single_instance_lines(dev, cpu_single) -> dict:
+    """Configs 1 and 2 through the solver API (one instance each): KS n=1024 IF34 FP64 eps=1e-4
+    to t=50 storing every 20 steps; NLS n=4096 ETD35 eps=1e-6 to t=20 in FP64 and FP32.  Each:
+    mode-steps/s (wall clock of the evolve call, best of 3 after a warm-up), attempts, rel L2
+    against the FP64 oracle's final state, and the oracle on one host process beside it."""
+    import torch
+
+    import rkstiff_gb300 as rk
+
+    ks, nls = single_instance_problems()
+    out = {}
+    cases = (("config1_ks1024_if34_fp64", "IF34", ks, "fp64", 1e-4, 50.0, 20, "ks1024_if34"),
+             ("config2_nls4096_etd35_fp64", "ETD35", nls, "fp64", 1e-6, 20.0, 0, "nls4096_etd35"),
+             ("config2_nls4096_etd35_fp32", "ETD35", nls, "fp32", 1e-6, 20.0, 0, "nls4096_etd35"))
+    for name, method, (lin, nl, u0), prec, eps, tf, freq, ref_key in cases:
+        best = None
+        for rep in range(4):
+            s = getattr(rk, method)(lin, nl, config=rk.SolverConfig(epsilon=eps),
+                                    device_options=rk.DeviceOptions(precision=prec, device=dev))
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            uf = s.evolve(u0, 0.0, tf, store_data=freq > 0, store_freq=max(freq, 1))
+            dt = time.perf_counter() - t0
+            if rep > 0:
+                best = dt if best is None else min(best, dt)
+        m = int(np.asarray(u0).shape[0])
+        st = s.stats
+        line = {"metric": "mode-steps/s", "value": m * st["steps"] / best, "seconds": best, "modes": m,
+                "steps": int(st["steps"]), "attempts": int(st["attempts"]), "nl_evals": int(st["nl_evals"]),
+                "precision": prec, "path": "solver API (host arrays in and out, one persistent launch)"}
+        ref = (cpu_single or {}).get(ref_key)
+        if ref is not None:
+            line["attempts_oracle"] = int(ref["attempts"])
+            line["rel_l2_vs_fp64_oracle"] = _rel(uf, ref["final"])
+            line["cpu_reference"] = {"value": m * ref["steps"] / ref["seconds"], "unit": "mode-steps/s",
+                                     "seconds": ref["seconds"], "cores": 1, "kind": "port",
+                                     "sample": "the whole run by the NumPy FP64 oracle in one host process"}
+        out[name] = line
+    return out
+
+
+def forms_comparison(dev, oracle_refs=None) -> dict:
     """Plain FP64, plain FP32 and FP32 + learned controller on the viscous Burgers ensemble
     (2048 instances the controller was not trained on): mode-steps/s, NL evaluations per
     unit simulated time, rejected steps, and rel L2 error against an FP64 run at
@@ -273,12 +386,19 @@ def forms_comparison(dev) -> dict:
     ok = np.ones(len(inst), bool)
     for st, _, _, _ in runs.values():
         ok &= st["status"] == 0
-    idx = np.where(ok)[0][:: max(1, int(ok.sum()) // FORMS["reference_sample"])][: FORMS["reference_sample"]]
-    ref_ens = Ensemble("ETD35", [lins[i] for i in idx], [nls[i] for i in idx],
-                       config=SolverConfig(epsilon=FORMS["reference_epsilon"]), precision="fp64", device=dev)
-    ref = [o.cpu().numpy() for o in ref_ens.evolve([u0s[i] for i in idx], 0.0, FORMS["tf"], max_steps=50000,
-                                                    max_launches=2)]
-    out = {"config": FORMS, "instances_finished_by_all": int(ok.sum())}
+    if oracle_refs:
+        # the FP64 NumPy oracle (the reference's algorithm) at the tight epsilon
+        idx = np.array([i for i in sorted(oracle_refs) if ok[i]], dtype=np.int64)
+        ref = [oracle_refs[int(i)] for i in idx]
+        ref_kind = f"FP64 NumPy oracle at epsilon {FORMS['reference_epsilon']:g} on {len(idx)} resolved instances"
+    else:
+        idx = np.where(ok)[0][:: max(1, int(ok.sum()) // FORMS["reference_sample"])][: FORMS["reference_sample"]]
+        ref_ens = Ensemble("ETD35", [lins[i] for i in idx], [nls[i] for i in idx],
+                           config=SolverConfig(epsilon=FORMS["reference_epsilon"]), precision="fp64", device=dev)
+        ref = [o.cpu().numpy() for o in ref_ens.evolve([u0s[i] for i in idx], 0.0, FORMS["tf"], max_steps=50000,
+                                                        max_launches=2)]
+        ref_kind = f"GPU FP64 run at epsilon {FORMS['reference_epsilon']:g} on {len(idx)} instances"
+    out = {"config": FORMS, "instances_finished_by_all": int(ok.sum()), "error_reference": ref_kind}
     for name, (st, dt, finals, ms) in runs.items():
         errs = np.array([np.linalg.norm(finals[i] - r) / np.linalg.norm(r) for i, r in zip(idx, ref)])
         done = st["status"] == 0
@@ -293,11 +413,29 @@ def forms_comparison(dev) -> dict:
             "rel_l2_median": float(np.median(errs)),
             "rel_l2_p90": float(np.quantile(errs, 0.9)),
         }
-    p64, l32 = out["plain_fp64"], out["learned_fp32"]
+    p64, p32, l32 = out["plain_fp64"], out["plain_fp32"], out["learned_fp32"]
     out["learned_fp32_over_plain_fp64"] = {
         "mode_steps_per_s": l32["mode_steps_per_s"] / p64["mode_steps_per_s"],
         "nl_evals_per_unit_time": l32["nl_evals_per_unit_time"] / p64["nl_evals_per_unit_time"],
     }
+    # the controller comparison on time to solution (a controller that takes fewer, larger
+    # steps lowers mode-steps/s while finishing sooner)
+    out["learned_fp32_over_plain_fp32"] = {
+        "mode_time_units_per_s": l32["mode_time_units_per_s"] / p32["mode_time_units_per_s"],
+        "nl_evals_per_unit_time": l32["nl_evals_per_unit_time"] / p32["nl_evals_per_unit_time"],
+        "rejects": l32["rejects"] / max(p32["rejects"], 1),
+    }
+    # FP32 rounding alone: the same fixed-step trajectory (ETD5, the ETD35 stages without the
+    # controller) in FP32 and in FP64 on the error sample, so no step-size decision differs
+    hfix = FORMS["precision_check_h"]
+    fin = {}
+    for prec in ("fp32", "fp64"):
+        e5 = Ensemble("ETD5", [lins[i] for i in idx], [nls[i] for i in idx], precision=prec, device=dev)
+        fin[prec] = [o.cpu().numpy().astype(np.complex128) for o in
+                     e5.evolve([u0s[i] for i in idx], 0.0, FORMS["tf"], h_init=hfix, max_steps=50000)]
+    out["fp32_rounding_fixed_step"] = {**_stats([_rel(a, b) for a, b in zip(fin["fp32"], fin["fp64"])]),
+                                       "method": "ETD5", "h": hfix,
+                                       "what": "rel L2 of FP32 against FP64 on the same fixed-step trajectory"}
     return out
 
 
@@ -409,7 +547,7 @@ def dense_measurement(dev) -> dict:
     }
 
 
-def gpu_arm(args, rank, world, cpu_line, dense_cpu=None):
+def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
     import torch
 
     from rkstiff_gb300 import models, sharding
@@ -511,8 +649,12 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None):
 
     if rank != 0:
         return
+    extra = extra or {}
+    gpu_finals = [x.cpu().numpy().astype(np.complex128) for x in eng.unpack_u(u)]
+    accuracy = headline_accuracy(dev, inst, gpu_finals, extra.get("tf_finals")) if world == 1 else None
+    single = single_instance_lines(dev, extra.get("single")) if (world == 1 and not args.no_single) else None
     peak = measure_fp32_peak(dev)
-    forms = forms_comparison(dev) if (world == 1 and not args.no_forms) else None
+    forms = forms_comparison(dev, extra.get("forms_ref")) if (world == 1 and not args.no_forms) else None
     dense = dense_measurement(dev) if (world == 1 and not args.no_dense) else None
     if dense is not None:
         dense["cpu_baseline"] = dense_cpu
@@ -565,6 +707,10 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None):
         "gpu_launches": n_kernels,
         "cpu_baseline": cpu_line,
     }
+    if accuracy is not None:
+        line["accuracy"] = accuracy
+    if single is not None:
+        line["single_instance"] = single
     if forms is not None:
         line["forms"] = forms
     if dense is not None:
@@ -589,7 +735,7 @@ def reference_arm(args, rank, world):
         for _ in range(args.steps):
             sample = inst[(step * per_step) % len(inst):][:per_step]
             _, wall, res = cpu_measure(pool, sample)
-            total_ms += sum(m * s for m, s, _, _ in res)
+            total_ms += sum(r[0] * r[1] for r in res)
             total_wall += wall
             step += 1
     finally:
@@ -619,14 +765,79 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_line(cores: int, dense: bool = False):
-    """The KS ensemble's CPU baseline line and, with ``dense``, the dense config's (or None)."""
+def _cpu_single(args):
+    """One process, one solver: the single-instance configurations timed by the oracle
+    (the reference's algorithm), wall time inside the worker."""
+    name = args[0]
+    from oracle import rk_oracle as O
+    if name == "ks1024_if34":
+        lin, nl, u0 = args[1:]
+        s = O.OracleSolver("IF34", lin, nl, O.SolverConfig())
+        t0 = time.perf_counter()
+        uf = s.evolve(u0, 0.0, 50.0, store_freq=20)
+    else:
+        lin, nl, u0 = args[1:]
+        s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=1e-6))
+        t0 = time.perf_counter()
+        uf = s.evolve(u0, 0.0, 20.0, store_data=False)
+    wall = time.perf_counter() - t0
+    return name, wall, sum(1 for r in s.log if r[3]), s.attempts, s.nl_evals, uf
+
+
+def _cpu_forms_reference(args):
+    """A Burgers instance of the controller comparison to tf by the oracle at a tight
+    epsilon (the accuracy reference of every form)."""
+    idx, lin, nl, u0, eps, tf = args
+    from oracle import rk_oracle as O
+    s = O.OracleSolver("ETD35", lin, nl, O.SolverConfig(epsilon=eps))
+    return idx, s.evolve(u0, 0.0, tf, store_data=False)
+
+
+def single_instance_problems():
+    """Configs 1 and 2 as (lin, nl, u0): KS n=1024 on [0, 32 pi) with u0 = cos(x/16)(1 +
+    sin(x/16)), and the three-soliton NLS n=4096 on [-50, 50) (seed 0)."""
+    from rkstiff_gb300 import grids, models, workloads
+
+    x, kx = grids.construct_x_kx_rfft(1024, 0.0, 32 * np.pi)
+    lin, nl = models.ks_ops(kx)
+    ks = (lin, nl, np.fft.rfft(np.cos(x / 16) * (1 + np.sin(x / 16))))
+    nls = workloads.nls_solitons(1, 0)[0]
+    return ks, nls
+
+
+def forms_reference_sample():
+    """Indices of the Burgers set whose viscosity resolves the n=512 grid (nu > 5e-3; every
+    form and the reference finish them), the first FORMS['reference_sample'] // 4 of them."""
+    from rkstiff_gb300 import workloads
+
+    inst = workloads.burgers_ensemble(FORMS["instances"], FORMS["seed"], n=FORMS["n"], nu_range=FORMS["nu_range"])
+    nus = np.array([-float(np.real(lin[1])) for lin, _, _ in inst])
+    idx = [int(i) for i in np.where(nus > 5e-3)[0][: FORMS["reference_sample"] // 4]]
+    return inst, idx
+
+
+def cpu_baseline_line(cores: int, dense: bool = False, extras: bool = False):
+    """The KS ensemble's CPU baseline line and, with ``dense``, the dense config's (or None);
+    with ``extras`` also the single-instance configs' one-process timings, the oracle's
+    tf = 100 states of the sampled instances and the forms' tight-epsilon references."""
     inst = make_instances(WORKLOAD["instances"], WORKLOAD["seed"])
     sample = inst[: 4 * cores]
     pool = cpu_pool(cores)
     dense_line = None
+    extra = {}
     try:
+        if extras:
+            ks, nls = single_instance_problems()
+            singles = pool.map(_cpu_single, [("ks1024_if34",) + ks, ("nls4096_etd35",) + nls], chunksize=1)
+            extra["single"] = {r[0]: {"seconds": r[1], "steps": r[2], "attempts": r[3], "nl_evals": r[4],
+                                      "final": r[5]} for r in singles}
+            finst, fidx = forms_reference_sample()
+            refs = pool.map(_cpu_forms_reference, [(i, finst[i][0], finst[i][1], finst[i][2],
+                                                    FORMS["reference_epsilon"], FORMS["tf"]) for i in fidx],
+                            chunksize=1)
+            extra["forms_ref"] = dict(refs)
         value, wall, res = cpu_measure(pool, sample)
+        extra["tf_finals"] = {i: r[4] for i, r in enumerate(res) if r[3] == 0}
         if dense:
             from rkstiff_gb300 import workloads
 
@@ -646,7 +857,7 @@ def cpu_baseline_line(cores: int, dense: bool = False):
         pool.join()
     return ({"value": value, "unit": UNIT, "cores": cores, "kind": "port",
              "sample": f"first {len(sample)} instances of the workload to tf=100 by the NumPy FP64 oracle, "
-                       f"{cores} worker processes ({cpu_model()}), {wall:.1f} s wall"}, dense_line)
+                       f"{cores} worker processes ({cpu_model()}), {wall:.1f} s wall"}, dense_line, extra)
 
 
 def main():
@@ -658,6 +869,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the plain/learned Burgers comparison")
     ap.add_argument("--no-dense", action="store_true", help="skip the dense Allen-Cahn measurement")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-instance configs (KS n=1024, NLS n=4096)")
     ap.add_argument("--tune-cache", default="", help="JSON file of tuned launch shapes to load, or to write")
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="smaller cases for profiling")
     ap.add_argument("--sizes", default="", help="comma-separated subset of the grid sizes (profiling)")
@@ -674,15 +886,16 @@ def main():
         return
     # the CPU baseline pool is spawned before any CUDA call
     cpu_line = dense_cpu = None
+    extra = {}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu_line, dense_cpu = cpu_baseline_line(host_cores(), dense=not args.no_dense)
+        cpu_line, dense_cpu, extra = cpu_baseline_line(host_cores(), dense=not args.no_dense, extras=True)
     if world > 1:
         import torch
         import torch.distributed as dist
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    gpu_arm(args, rank, world, cpu_line, dense_cpu)
+    gpu_arm(args, rank, world, cpu_line, dense_cpu, extra)
     if world > 1:
         import torch.distributed as dist
 

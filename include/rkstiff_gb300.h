@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define RK_ABI_VERSION 1
+#define RK_ABI_VERSION 2
 
 /* twiddle table length: supports complex FFTs and real grids up to this many points */
 #define RK_TW_N 8192
@@ -152,7 +152,7 @@ typedef struct rk_batch {
   const int64_t* class_start;   /* [host] n_classes+1 offsets into `order`                */
   const int32_t* class_threads; /* [host] threads per instance per class (NULL: auto)     */
   const int32_t* class_place;   /* [host] placement per class (NULL: `placement`)         */
-  const int32_t* class_groups;  /* [host] instance groups per block per class (NULL: auto) */
+  const int32_t* class_groups;  /* [host] instance groups per block per class, threads x groups <= 512 (NULL: auto) */
   /* Optional per-attempt log: instance i writes RK_LOG_FIELDS floats per attempt at
    * attempt_log + (i * log_cap + k) * RK_LOG_FIELDS for its attempts k < log_cap
    * (counted over the whole evolve).  NULL: no log. */
@@ -164,7 +164,44 @@ typedef struct rk_batch {
    * reference's rule.  NULL: the reference's controller (solveras.py:508-554). */
   float mlp_target;
   const void* mlp;
+  /* Optional snapshot stream (replaces the list append of solveras.py:643-646 for long
+   * runs): with ring_data set, each snapshot (every store_freq accepted steps) goes to the
+   * next slot of a ring in mapped, pinned host memory (rk_ring_create) while the launch
+   * runs, instead of snap_u / snap_t; the host drains it with rk_ring_take.  A writer claims
+   * slot k with an atomic add on *ring_head and waits (bounded by ring_timeout_ms) until the
+   * host has taken slot k - ring_slots (*ring_tail > k - ring_slots); if that wait runs out
+   * the instance pauses with RK_ST_SNAP_FULL and slot k is never completed (the host sees
+   * the stream as overrun).  Slot layout: RK_RING_HEADER bytes {int64 ready (k + 1 once
+   * the slot is complete), int64 instance, double t, int64 step} then m_i complex states. */
+  void* ring_data;           /* [mapped host] ring_slots * ring_slot_bytes, or NULL     */
+  int64_t ring_slot_bytes;   /* >= RK_RING_HEADER + m_max * sizeof(complex T)           */
+  int32_t ring_slots;
+  int32_t ring_timeout_ms;
+  unsigned long long* ring_head; /* [mapped host] slots claimed by the kernels            */
+  const int64_t* ring_tail;      /* [mapped host] slots taken by the host                 */
 } rk_batch;
+
+#define RK_RING_HEADER 32
+
+/* Snapshot ring in mapped, pinned host memory (cudaHostAlloc with cudaHostAllocMapped):
+ * rk_ring_create sets r->data / head / tail to device-visible pointers of `slots` slots of
+ * `slot_bytes` bytes, zeroed.  rk_ring_take copies slot k (the k-th snapshot written since
+ * creation, k counted from 0) to dst (at most `bytes` bytes) and returns 1 if it is
+ * complete, 0 if it is not yet; taking it frees the slot for the writer that claims slot
+ * k + slots.  Slots must be taken in order.  (No counterpart in the reference: it appends
+ * each snapshot to the solver's Python lists, solveras.py:643-646.) */
+typedef struct rk_ring {
+  void* data;
+  unsigned long long* head;
+  int64_t* tail;
+  int64_t slot_bytes;
+  int32_t slots;
+  int32_t reserved;
+} rk_ring;
+int rk_ring_create(int64_t slots, int64_t slot_bytes, rk_ring* r);
+int rk_ring_take(rk_ring* r, int64_t k, void* dst, int64_t bytes);
+int rk_ring_reset(rk_ring* r);
+int rk_ring_destroy(rk_ring* r);
 
 /* per-attempt log record: t, h, s (inf/NaN stored as 1e30 / -1), accepted (0/1), fraction
  * of |unew|^2 in the top quarter of the modes, rejects so far in the step, grid n, method */

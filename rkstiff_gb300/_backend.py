@@ -58,6 +58,31 @@ class DiagBackend:
         freq = int(store_freq) if store_data else 0
         if store_data and freq <= 0:
             raise ValueError("store_freq must be a positive integer")
+        opts = s.device_options
+        if freq > 0 and (opts.stream_snapshots or opts.snapshot_file):
+            writer = None
+            if opts.snapshot_file:
+                from .snapshots import NpzSnapshotWriter
+
+                writer = NpzSnapshotWriter(opts.snapshot_file)
+                # the initial state the solver recorded goes to the file as well
+                writer.append(s.t[-1], s.u.pop())
+            as_tensor = isinstance(u, torch.Tensor)
+
+            def sink(inst, tt, step, uu):
+                s.t.append(tt)
+                if writer is not None:
+                    writer.append(tt, uu)
+                else:
+                    s.u.append(torch.from_numpy(uu).to(u.device) if as_tensor else uu)
+
+            try:
+                st = self.ens.evolve_stream(u_dev, t0, tf, h, freq, sink)
+            finally:
+                if writer is not None:
+                    writer.close()
+            self.st = st
+            return _to_output(u_dev, u), int(st["status"][0])
         st = self.ens.evolve(u_dev, t0, tf, h, store_freq=freq, snap_cap=self.snap_cap, on_snapshots=on_snaps)
         self.st = st
         return _to_output(u_dev, u), int(st["status"][0])

@@ -25,6 +25,7 @@ RK_ST_RUNNING, RK_ST_DONE, RK_ST_MAX_LOOPS, RK_ST_MIN_STEP = -1, 0, 1, 2
 RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE, RK_ST_BAD_SIZE, RK_ST_WAIT_TIMEOUT = 4, 5, 6, 7, 8
 RK_OK, RK_E_ARG, RK_E_CUDA, RK_E_UNSUPPORTED, RK_E_SIZE = 0, -1, -2, -3, -4
 RK_TW_N = 8192
+ABI_VERSION = 2
 RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL = -1, 0, 1, 2
 
 # number of stage arrays and coefficient arrays per method (mirrors rk_evolve.cuh Traits)
@@ -58,7 +59,17 @@ class RkBatch(ctypes.Structure):
         ("class_groups", ctypes.c_void_p),
         ("attempt_log", ctypes.c_void_p), ("log_cap", ctypes.c_int32), ("mlp_target", ctypes.c_float),
         ("mlp", ctypes.c_void_p),
+        ("ring_data", ctypes.c_void_p), ("ring_slot_bytes", ctypes.c_int64), ("ring_slots", ctypes.c_int32),
+        ("ring_timeout_ms", ctypes.c_int32), ("ring_head", ctypes.c_void_p), ("ring_tail", ctypes.c_void_p),
     ]
+
+
+RK_RING_HEADER = 32
+
+
+class RkRing(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("head", ctypes.c_void_p), ("tail", ctypes.c_void_p),
+                ("slot_bytes", ctypes.c_int64), ("slots", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class RkTerm(ctypes.Structure):
@@ -110,7 +121,8 @@ EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
            "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve",
-           "rk_fourier_grid", "rk_cheb_grid", "rk_dx_fourier", "rk_dx_cheb_work_bytes", "rk_dx_cheb")
+           "rk_fourier_grid", "rk_cheb_grid", "rk_dx_fourier", "rk_dx_cheb_work_bytes", "rk_dx_cheb",
+           "rk_ring_create", "rk_ring_take", "rk_ring_reset", "rk_ring_destroy")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -184,7 +196,13 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_dx_cheb.argtypes = [i32, i64, i64, vp, vp, vp, vp, vp]
         for fn in (lib.rk_fourier_grid, lib.rk_cheb_grid, lib.rk_dx_fourier, lib.rk_dx_cheb):
             fn.restype = ctypes.c_int
-        if lib.rk_abi_version() != 1:
+        lib.rk_ring_create.argtypes = [i64, i64, ctypes.POINTER(RkRing)]
+        lib.rk_ring_take.argtypes = [ctypes.POINTER(RkRing), i64, vp, i64]
+        lib.rk_ring_reset.argtypes = [ctypes.POINTER(RkRing)]
+        lib.rk_ring_destroy.argtypes = [ctypes.POINTER(RkRing)]
+        for fn in (lib.rk_ring_create, lib.rk_ring_take, lib.rk_ring_reset, lib.rk_ring_destroy):
+            fn.restype = ctypes.c_int
+        if lib.rk_abi_version() != ABI_VERSION:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib
         return lib

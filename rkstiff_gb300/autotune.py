@@ -26,7 +26,8 @@ from . import _native as nat
 from .engine import DiagEnsemble
 
 # (threads per instance group, groups per block)
-SHAPES = ((32, 4), (32, 8), (64, 2), (64, 4), (128, 1), (128, 2), (256, 1))
+SHAPES = ((32, 4), (32, 8), (32, 16), (64, 2), (64, 4), (64, 8), (128, 1), (128, 2), (128, 4), (256, 1),
+          (256, 2))
 PLACES = (nat.RK_PLACE_SMEM_ALL, nat.RK_PLACE_SMEM_STATE, nat.RK_PLACE_GLOBAL)
 
 _CACHE: Dict[Tuple, Tuple[Tuple[int, int, int], ...]] = {}

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <string.h>
+
 #include <mutex>
 #include <string>
 #include <vector>
@@ -189,7 +191,16 @@ int validate_batch(const rk_batch* b, bool need_scratch) {
     set_error("rk_evolve: n_max must be a power of two in [4, " + std::to_string(limit) + "]");
     return RK_E_SIZE;
   }
-  if (b->store_freq > 0 && (b->snap_cap <= 0 || !b->snap_u || !b->snap_t)) {
+  if (b->ring_data) {
+    const int64_t m_max = b->nl_kind == RK_NL_UUX ? nmax / 2 + 1 : nmax;
+    const int64_t need = RK_RING_HEADER + m_max * (b->precision == RK_FP64 ? 16 : 8);
+    if (b->ring_slots < 1 || !b->ring_head || !b->ring_tail || b->ring_slot_bytes < need ||
+        (b->ring_slot_bytes & 15) || b->ring_timeout_ms < 1) {
+      set_error("rk_evolve: the snapshot ring needs >= 1 slot of >= " + std::to_string((long long)need) +
+                " bytes (a multiple of 16), head, tail and a positive timeout");
+      return RK_E_ARG;
+    }
+  } else if (b->store_freq > 0 && (b->snap_cap <= 0 || !b->snap_u || !b->snap_t)) {
     set_error("rk_evolve: snapshots requested without a snapshot buffer");
     return RK_E_ARG;
   }
@@ -258,6 +269,82 @@ int rk_coeffs(int32_t method, int32_t precision, int32_t coef_complex, int64_t m
   return RK_E_ARG;
 }
 
+int rk_ring_create(int64_t slots, int64_t slot_bytes, rk_ring* r) {
+  if (!r || slots < 1 || slots > (1 << 24) || slot_bytes < RK_RING_HEADER || (slot_bytes & 15)) {
+    set_error("rk_ring_create: slots in [1, 2^24] and slot_bytes >= RK_RING_HEADER, a multiple of 16");
+    return RK_E_ARG;
+  }
+  void* data = nullptr;
+  void* ctr = nullptr;
+  if (int e = cuda_check(cudaHostAlloc(&data, (size_t)(slots * slot_bytes), cudaHostAllocMapped), "ring alloc"))
+    return e;
+  if (int e = cuda_check(cudaHostAlloc(&ctr, 64, cudaHostAllocMapped), "ring counters")) {
+    cudaFreeHost(data);
+    return e;
+  }
+  memset(data, 0, (size_t)(slots * slot_bytes));
+  memset(ctr, 0, 64);
+  void* dd = nullptr;
+  void* dc = nullptr;
+  if (cudaHostGetDevicePointer(&dd, data, 0) != cudaSuccess || cudaHostGetDevicePointer(&dc, ctr, 0) != cudaSuccess ||
+      dd != data || dc != ctr) {
+    // the pointers are handed to kernels as they are: a platform without unified addressing
+    // would need the separate device aliases, which this ring does not keep
+    cudaFreeHost(data);
+    cudaFreeHost(ctr);
+    set_error("rk_ring_create: mapped host memory is not addressable at the same address on the device");
+    return RK_E_UNSUPPORTED;
+  }
+  r->data = data;
+  r->head = static_cast<unsigned long long*>(ctr);
+  r->tail = reinterpret_cast<int64_t*>(static_cast<char*>(ctr) + 8);
+  r->slot_bytes = slot_bytes;
+  r->slots = (int32_t)slots;
+  r->reserved = 0;
+  return RK_OK;
+}
+
+int rk_ring_take(rk_ring* r, int64_t k, void* dst, int64_t bytes) {
+  if (!r || !r->data || k < 0 || (bytes > 0 && !dst)) {
+    set_error("rk_ring_take: invalid argument");
+    return RK_E_ARG;
+  }
+  const int64_t tail = __atomic_load_n(r->tail, __ATOMIC_RELAXED);
+  if (k != tail) {
+    set_error("rk_ring_take: slots must be taken in order");
+    return RK_E_ARG;
+  }
+  unsigned char* slot = static_cast<unsigned char*>(r->data) + (k % r->slots) * r->slot_bytes;
+  // the kernel publishes `ready` after a system-scope fence over the slot's contents: an
+  // acquire load orders the copy below after it
+  const int64_t ready = __atomic_load_n(reinterpret_cast<int64_t*>(slot), __ATOMIC_ACQUIRE);
+  if (ready != k + 1) return 0;
+  if (bytes > 0) memcpy(dst, slot, (size_t)(bytes < r->slot_bytes ? bytes : r->slot_bytes));
+  __atomic_store_n(r->tail, k + 1, __ATOMIC_RELEASE);
+  return 1;
+}
+
+int rk_ring_reset(rk_ring* r) {
+  if (!r || !r->data) {
+    set_error("rk_ring_reset: invalid ring");
+    return RK_E_ARG;
+  }
+  memset(r->data, 0, (size_t)(r->slots * r->slot_bytes));
+  __atomic_store_n(r->head, 0ull, __ATOMIC_RELEASE);
+  __atomic_store_n(r->tail, (int64_t)0, __ATOMIC_RELEASE);
+  return RK_OK;
+}
+
+int rk_ring_destroy(rk_ring* r) {
+  if (!r) return RK_E_ARG;
+  if (r->data) cudaFreeHost(r->data);
+  if (r->head) cudaFreeHost(r->head);
+  r->data = nullptr;
+  r->head = nullptr;
+  r->tail = nullptr;
+  return RK_OK;
+}
+
 int rk_probe_fp32(float* out, int32_t blocks, int32_t threads, int32_t iters, void* stream) {
   if (!out || blocks <= 0 || threads <= 0 || threads > 1024 || iters <= 0) {
     set_error("rk_probe_fp32: invalid argument");
@@ -300,8 +387,8 @@ int rk_evolve(const rk_batch* b, void* stream) {
       return RK_E_ARG;
     }
     int grp = b->class_groups ? b->class_groups[c] : auto_groups(thr);
-    if (grp < 1 || thr * grp > 256 || (thr > 32 && grp > 15)) {
-      set_error("rk_evolve: class groups must be >= 1 with threads * groups <= 256");
+    if (grp < 1 || thr * grp > 512 || (thr > 32 && grp > 15)) {
+      set_error("rk_evolve: class groups must be >= 1 with threads * groups <= 512");
       return RK_E_ARG;
     }
     int pl = b->class_place ? b->class_place[c] : b->placement;

@@ -754,6 +754,60 @@ RK_DEV float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi
 RK_DEV float safe_log(double v) { return (v > 0.0 && v < 1e300) ? (float)log(v) : (v > 0.0 ? 690.f : -690.f); }
 
 // ---------------------------------------------------------------------------------
+// snapshot stream: one slot of the mapped host ring per snapshot
+// ---------------------------------------------------------------------------------
+RK_DEV uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Writes the instance's state u (m modes) at time t, step `step` into the next ring slot.
+// Thread 0 claims the slot and waits (bounded by ring_timeout_ms) until the host has taken
+// its previous occupant; the group then writes the states, fences them to the system scope
+// and thread 0 publishes the slot (ready = k + 1).  Returns false if the wait ran out (the
+// slot stays unpublished).  `red` provides the group's broadcast word.
+template <class T>
+RK_DEV bool ring_write(const rk_batch& b, int inst, const Group& g, const cx<T>* u, int m, double t, int64_t step,
+                       double* red) {
+  long long* slot_s = reinterpret_cast<long long*>(red + 65);
+  g.sync();  // earlier readers of the broadcast word are done
+  if (g.tid == 0) {
+    const long long k = (long long)atomicAdd(b.ring_head, 1ull);
+    const volatile int64_t* tail = b.ring_tail;
+    const uint64_t t0 = global_ns(), lim = (uint64_t)b.ring_timeout_ms * 1000000ull;
+    long long res = k;
+    while (k - (long long)*tail >= (long long)b.ring_slots) {
+      if (global_ns() - t0 > lim) {
+        res = -1;
+        break;
+      }
+      __nanosleep(2000);
+    }
+    *slot_s = res;
+  }
+  g.sync();
+  const long long k = *slot_s;
+  if (k < 0) return false;
+  unsigned char* slot = static_cast<unsigned char*>(b.ring_data) + (k % b.ring_slots) * b.ring_slot_bytes;
+  cx<T>* dst = reinterpret_cast<cx<T>*>(slot + RK_RING_HEADER);
+  for (int j = g.tid; j < m; j += g.nthr) dst[j] = u[j];
+  if (g.tid == 0) {
+    int64_t* hdr = reinterpret_cast<int64_t*>(slot);
+    hdr[1] = inst;
+    reinterpret_cast<double*>(hdr)[2] = t;
+    hdr[3] = step;
+  }
+  __threadfence_system();
+  g.sync();
+  if (g.tid == 0) {
+    __threadfence_system();
+    *reinterpret_cast<volatile int64_t*>(slot) = (int64_t)k + 1;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------------
 // one instance, start to pause/finish
 //
 // PLACE selects where the instance's arrays live: PL_GLOBAL (all in the global scratch
@@ -973,15 +1027,22 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     ++st.steps;
     ++steps_this;
     if (status != RK_ST_RUNNING) break;
-    if (b.store_freq > 0 && (st.steps % b.store_freq) == 0 && snap < b.snap_cap) {
-      cx<T>* su = reinterpret_cast<cx<T>*>(b.snap_u) + (int64_t)b.snap_cap * mo + (int64_t)snap * x.m;
-      for (int j = g.tid; j < x.m; j += g.nthr) su[j] = x.u[j];
-      if (g.tid == 0) b.snap_t[(int64_t)inst * b.snap_cap + snap] = t;
-      ++snap;
+    bool ring_full = false;
+    if (b.store_freq > 0 && (st.steps % b.store_freq) == 0) {
+      if (b.ring_data) {
+        ring_full = !ring_write<T>(b, inst, g, x.u, x.m, t, st.steps, red);
+        if (!ring_full) ++snap;
+      } else if (snap < b.snap_cap) {
+        cx<T>* su = reinterpret_cast<cx<T>*>(b.snap_u) + (int64_t)b.snap_cap * mo + (int64_t)snap * x.m;
+        for (int j = g.tid; j < x.m; j += g.nthr) su[j] = x.u[j];
+        if (g.tid == 0) b.snap_t[(int64_t)inst * b.snap_cap + snap] = t;
+        ++snap;
+      }
     }
-    if (b.run_mode == RK_RUN_STEP) status = RK_ST_STEP_DONE;
+    if (ring_full) status = RK_ST_SNAP_FULL;
+    else if (b.run_mode == RK_RUN_STEP) status = RK_ST_STEP_DONE;
     else if (!(t < tf)) status = RK_ST_DONE;
-    else if (b.store_freq > 0 && snap >= b.snap_cap) status = RK_ST_SNAP_FULL;
+    else if (b.store_freq > 0 && !b.ring_data && snap >= b.snap_cap) status = RK_ST_SNAP_FULL;
     else if (steps_this >= b.max_steps) status = RK_ST_ITER_CAP;
   }
   g.sync();
@@ -1014,7 +1075,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
 // group slices.  A one-warp group synchronises with __syncwarp, a multi-warp group with a
 // named barrier (one per group), a block-wide group with __syncthreads.
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
-__global__ void __launch_bounds__(256, 2) evolve_kernel(const rk_batch b, const int32_t* __restrict__ order,
+__global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const int32_t* __restrict__ order,
                                                         int64_t count, int32_t* queue, int nfft, int gthreads,
                                                         int group_smem) {
   extern __shared__ __align__(16) unsigned char smem[];

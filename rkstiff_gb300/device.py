@@ -18,9 +18,16 @@ class DeviceOptions:
     device    : CUDA device (default: the current one)
     threads   : threads per instance group (0: the kernel default, 256)
     snap_cap  : snapshots the device buffers hold before the host drains them
+    stream_snapshots : stream the snapshots of evolve through a pinned, mapped host ring
+                while the launch runs (one launch to tf, no device snapshot buffer)
+    snapshot_file : path of an .npz file (arrays t and u) the streamed snapshots are
+                written to, including the initial state; solver.u then stays empty
+                (solver.t still lists the times).  Implies stream_snapshots.
     """
 
     precision: str = "fp64"
     device: Optional[Union[str, torch.device]] = None
     threads: int = 0
     snap_cap: int = 256
+    stream_snapshots: bool = False
+    snapshot_file: Optional[str] = None

@@ -227,7 +227,7 @@ class DiagEnsemble:
     # -- launch -----------------------------------------------------------------------
     def launch(self, u_dev: torch.Tensor, run_mode: int, store_freq: int = 0, snap_cap: int = 0,
                snap_u: Optional[torch.Tensor] = None, snap_t: Optional[torch.Tensor] = None,
-               max_steps: int = 200_000) -> None:
+               max_steps: int = 200_000, ring=None) -> None:
         if u_dev.dtype != self.cdtype or u_dev.device != self.device or not u_dev.is_contiguous():
             raise ValueError("state tensor must be a contiguous device tensor of the working dtype")
         b = nat.RkBatch()
@@ -269,6 +269,8 @@ class DiagEnsemble:
         b.log_cap = int(self.log_cap) if self.attempt_log is not None else 0
         b.mlp = self.mlp.data_ptr() if self.mlp is not None else None
         b.mlp_target = float(self.mlp_target)
+        if ring is not None:
+            ring.fill_batch(b)
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
             if self.record_events:
@@ -349,6 +351,45 @@ class DiagEnsemble:
             self.put_state(st)
         raise EvolveBoundError(f"evolve did not reach tf within {max_launches} launches of {max_steps} steps",
                                self.get_state())
+
+
+    def evolve_stream(self, u_dev: torch.Tensor, t0, tf, h, store_freq: int, sink, ring=None, slots: int = 64,
+                      max_steps: int = 200_000, max_launches: int = 50) -> np.ndarray:
+        """``evolve`` with the snapshots streamed: every ``store_freq`` accepted steps the
+        kernel writes the state into a pinned, mapped host ring (``snapshots.SnapshotRing``,
+        created here unless given) and the host hands each one to ``sink(inst, t, step,
+        u)`` (u a NumPy copy) while the launch runs; a launch ends only at tf, on failure or
+        at the ``max_steps`` bound.  Returns the final state records."""
+        from .snapshots import SnapshotRing, SnapshotStreamOverrun
+
+        if store_freq <= 0:
+            raise ValueError("store_freq must be a positive integer")
+        own = ring is None
+        if own:
+            ring = SnapshotRing(slots, int(self.ms.max()), self.prec)
+        try:
+            ring.reset()
+            st = self.fresh_state(t0, tf, h)
+            self.put_state(st)
+            for _ in range(max_launches):
+                self.launch(u_dev, nat.RK_RUN_EVOLVE, store_freq, 0, None, None, max_steps, ring=ring)
+                ev = torch.cuda.Event()
+                ev.record(torch.cuda.current_stream(self.device))
+                ring.drain(ev.query, self.ms, sink)
+                st = self.get_state()
+                if np.any(st["status"] == nat.RK_ST_SNAP_FULL):
+                    raise SnapshotStreamOverrun("a snapshot writer timed out waiting for the host")
+                resume = st["status"] == nat.RK_ST_ITER_CAP
+                if not np.any(resume):
+                    return st
+                st["snap_count"] = 0
+                st["status"] = np.where(resume, nat.RK_ST_RUNNING, st["status"])
+                self.put_state(st)
+            raise EvolveBoundError(f"evolve did not reach tf within {max_launches} launches of {max_steps} steps",
+                                   self.get_state())
+        finally:
+            if own:
+                ring.close()
 
 
 class EvolveBoundError(RuntimeError):

@@ -76,8 +76,14 @@ def test_dx_fft_reference_cases(golden):
     v = np.sin(x)
     for _ in range(4):
         v = dv.dx_fft(kx, v)
-    assert close(v, g["dfft_many4"], 1e-12)
-    assert close(dv.dx_fft(kx, np.sin(x), 8), g["dfft_order8"], 1e-12)
+    # four differentiations amplify rounding by up to max|kx|^4 ~ 1.7e7, an eighth-order
+    # one by ~3e14: these follow the reference's own tolerances against the exact
+    # derivative (tests/test_derivatives_fft.py:9-26), and the reference's output to the
+    # same amplified rounding
+    assert np.linalg.norm(v - np.sin(x)) / np.linalg.norm(np.sin(x)) < 1e-6
+    assert close(v, g["dfft_many4"], 1e-7)
+    v8 = dv.dx_fft(kx, np.sin(x), 8)
+    assert np.linalg.norm(v8 - np.sin(x)) / np.linalg.norm(np.sin(x)) < 0.1
     x, kx = grids.construct_x_kx_fft(100, 0, 2 * np.pi)
     assert close(dv.dx_fft(kx, np.sin(x)), g["dfft_periodic100"], 1e-13)
     x, kx = grids.construct_x_kx_fft(400, -30.0, 30.0)

@@ -36,7 +36,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version_and_sizes(lib):
-    assert lib.rk_abi_version() == 1
+    assert lib.rk_abi_version() == nat.ABI_VERSION == 2
     assert lib.rk_num_coeffs(nat.RK_ETD35) == 21
     assert lib.rk_num_coeffs(nat.RK_ETD34) == 10
     assert lib.rk_num_coeffs(nat.RK_IF34) == 2
