@@ -231,7 +231,7 @@ def measure_fp32_peak(device) -> float:
 
 FORMS = {"workload": "burgers_ensemble_etd35", "instances": 2048, "n": 512, "nu_range": [1e-3, 1e-1],
          "epsilon": 1e-5, "tf": 5.0, "seed": 7, "reference_epsilon": 1e-10, "reference_sample": 256,
-         "precision_check_h": 0.005}
+         "precision_check_h": 0.02}
 
 # accuracy of the headline (FP32) against the FP64 oracle on a sample: one adaptive step from
 # u0 (the <= 1e-6 gate), and trajectories to a short horizon; chaotic KS at tf = 100 is

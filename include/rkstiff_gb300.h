@@ -451,6 +451,25 @@ int64_t rk_dx_cheb_work_bytes(int64_t n);
 int rk_dx_cheb(int32_t order, int64_t n, int64_t cols, const double* D, const double* u, double* out, void* work,
                void* stream);
 
+/* Multi-dimensional NLS nonlinearities of the reference's NLS demo (demos/nls.ipynb cells
+ * 6-29, which evaluate them with numpy.fft and the Hankel matrix product of
+ * rkstiff/transforms.py:178-240) on the library's own kernels.  [device] arrays, complex in
+ * the precision's type (complex128 / complex64).
+ *   rk_nls_lines: along each of `lines` lines of n points (a power of two <= RK_TW_N; FP64 <=
+ *       4096), line l's point j at in[l * line_stride + j * elem_stride]: mode 0 the inverse
+ *       FFT (scaled by 1/n, numpy.fft.ifft), 1 the forward FFT, 2 the NLS step
+ *       fft(i gamma |v|^2 v) with v = ifft(x) -- one launch, the line held in shared memory.
+ *       n = 1 with mode 2 is the product i gamma |x|^2 x over `lines` contiguous points.  out
+ *       may alias in.  twiddle: the RK_TW_N table of rk_fill_twiddles in the precision.
+ *   rk_dht: the discrete Hankel transform over the radial axis: out = (Y in) * scale
+ *       (divide = 0, ht) or (Y in) / scale (divide = 1, iht) for Y the real n x n matrix
+ *       (row-major, in the precision's real type) and in / out n x w real, row-major (a
+ *       complex array of c columns is w = 2c real columns); out must not alias in. */
+int rk_nls_lines(int32_t precision, int32_t mode, int64_t n, int64_t lines, int64_t elem_stride, int64_t line_stride,
+                 double gamma, const void* in, void* out, const void* twiddle, void* stream);
+int rk_dht(int32_t precision, int32_t divide, int64_t n, int64_t w, const void* Y, double scale, const void* in,
+           void* out, void* stream);
+
 /* Measurement utility (no counterpart in the reference): `blocks` x `threads` threads
  * each run 8 independent FP32 FMA chains of `iters` steps and write one float to
  * out[blocks*threads] [device].  FLOPs = 16 * blocks * threads * iters; timing it gives the

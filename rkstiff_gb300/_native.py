@@ -122,7 +122,7 @@ EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
            "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve",
            "rk_fourier_grid", "rk_cheb_grid", "rk_dx_fourier", "rk_dx_cheb_work_bytes", "rk_dx_cheb",
-           "rk_ring_create", "rk_ring_take", "rk_ring_reset", "rk_ring_destroy")
+           "rk_ring_create", "rk_ring_take", "rk_ring_reset", "rk_ring_destroy", "rk_nls_lines", "rk_dht")
 RK_LOG_FIELDS = 8
 RK_MLP_IN, RK_MLP_H = 8, 64
 RK_MLP_NPARAM = RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1
@@ -202,6 +202,10 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_ring_destroy.argtypes = [ctypes.POINTER(RkRing)]
         for fn in (lib.rk_ring_create, lib.rk_ring_take, lib.rk_ring_reset, lib.rk_ring_destroy):
             fn.restype = ctypes.c_int
+        lib.rk_nls_lines.argtypes = [i32, i32, i64, i64, i64, i64, dbl, vp, vp, vp, vp]
+        lib.rk_nls_lines.restype = ctypes.c_int
+        lib.rk_dht.argtypes = [i32, i32, i64, i64, vp, dbl, vp, vp, vp]
+        lib.rk_dht.restype = ctypes.c_int
         if lib.rk_abi_version() != ABI_VERSION:
             raise RuntimeError("rkstiff_gb300 native library ABI mismatch")
         _lib = lib

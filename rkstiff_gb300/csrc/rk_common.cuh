@@ -148,6 +148,35 @@ RK_DEV void group_sum2_df(const Group& g, double* red, df a, df b, double& sa, d
   sb = (double)tb.hi + (double)tb.lo;
 }
 
+// group-wide double-float sums of two values, kept as double-float pairs (no FP64 at all)
+RK_DEV void group_sum2_dff(const Group& g, double* red, df a, df b, df& sa, df& sb) {
+  a = warp_sum_df(a);
+  b = warp_sum_df(b);
+  const int nw = g.nthr >> 5;
+  if (nw == 1) {
+    sa = a;
+    sb = b;
+    return;
+  }
+  float* rf = reinterpret_cast<float*>(red);
+  const int w = g.tid >> 5;
+  g.sync();
+  if ((g.tid & 31) == 0) {
+    rf[4 * w] = a.hi;
+    rf[4 * w + 1] = a.lo;
+    rf[4 * w + 2] = b.hi;
+    rf[4 * w + 3] = b.lo;
+  }
+  g.sync();
+  df ta{0.f, 0.f}, tb{0.f, 0.f};
+  for (int i = 0; i < nw; ++i) {
+    ta = df_add(ta, df{rf[4 * i], rf[4 * i + 1]});
+    tb = df_add(tb, df{rf[4 * i + 2], rf[4 * i + 3]});
+  }
+  sa = ta;
+  sb = tb;
+}
+
 // group-wide max of a non-negative FP32 value; NaN anywhere gives NaN
 RK_DEV float group_max_nan_f(const Group& g, double* red, float v, bool nan) {
   v = warp_max_f(nan ? 0.f : v);

@@ -59,6 +59,15 @@ RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m)
   return traits_nv(method) * vec + num_coeffs(method) * coef + kxw;
 }
 
+// FP32 controller constants, formed once per instance run so that no attempt needs FP64
+// arithmetic for them: cutoff^2 for the mask, log2(epsilon^2), safety
+struct CtlF {
+  float cut2, log2_eps2, safety;
+};
+RK_DEV CtlF make_ctlf(const rk_controller& c) {
+  return CtlF{(float)(c.adapt_cutoff * c.adapt_cutoff), (float)(2.0 * log2(c.epsilon)), (float)c.safety_f};
+}
+
 // ---------------------------------------------------------------------------------
 // per-instance working context
 // ---------------------------------------------------------------------------------
@@ -80,6 +89,7 @@ struct Ctx {
   double* red;
   const cx<T>* tw;   // global table of RK_TW_N twiddles
   const cx<T>* tws;  // compile-time path: shared-memory table of 2^LOGN twiddles
+  CtlF cf;           // FP32 controller constants (FP32 working precision)
   RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
 };
 
@@ -470,6 +480,25 @@ RK_DEV double s_from_sums_f32(double su, double se, const rk_controller& ctl, in
   return ctl.safety_f * (double)exp2f(log2f(rf) * (0.5f / (float)q));
 }
 
+// The same s from double-float sums with FP32 instructions only: log2 of the ratio as
+// log2(eps^2) + log2(su) - log2(se) (the pairs' high words carry the sums to FP32
+// precision, which bounds s's precision anyway), clamped where the ratio passes 1e30, and
+// the edge values of s_from_sums_f32: 0/0 and x/0 = inf reject (x/0 with |u| > 0 finite
+// takes MAX_S = 4, see above), a zero |u| gives s = 0.  log2_eps2 = log2(epsilon^2).
+RK_DEV double s_from_sums_f32_fast(df su, df se, float log2_eps2, float safety, int q) {
+  const float u = su.hi + su.lo, e = se.hi + se.lo;
+  const double inf = __longlong_as_double(0x7ff0000000000000ULL);
+  if (u != u || e != e) return nan_d();
+  if (e == 0.f) {
+    if (u > 0.f && !isinf(u)) return 4.0;  // below FP32 resolution, see above
+    return u == 0.f ? nan_d() : inf;      // 0/0, inf/0
+  }
+  if (isinf(u)) return isinf(e) ? nan_d() : inf;
+  if (u == 0.f || isinf(e)) return 0.0;
+  const float l = fminf(log2_eps2 + (log2f(u) - log2f(e)), 99.65784f);  // log2(1e30)
+  return (double)(safety * exp2f(l * (0.5f / (float)q)));
+}
+
 // s = safety (eps |unew[mask]| / |err[mask]|)^(1/q), mask = |unew| / max|unew| > cutoff
 // (rkstiff/solveras.py:451-455).  The sums of squares are accumulated in FP64.  In FP32
 // working precision the mask is evaluated on squared magnitudes, |u|^2 > cutoff^2 max|u|^2,
@@ -519,7 +548,7 @@ RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const 
 // known; then the masked sums from those two floats per mode.  Same values as write_unew
 // followed by controller_s, without the second pass over the stage vectors.
 template <class T, class CT, int LOGN, class KF, class EF>
-RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const rk_controller& ctl, int q) {
+RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const CtlF& cf, int q) {
   float* park = reinterpret_cast<float*>(x.fa);  // [2 m] floats: the buffer holds >= n complex
   x.g.sync();  // the last transform has released the buffer
   float mx = 0.f;
@@ -534,9 +563,9 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const rk_c
     park[2 * j] = a2;
     park[2 * j + 1] = e.x * e.x + e.y * e.y;
   }
-  const double maxu = (double)group_max_nan_f(x.g, x.red, mx, nan);
+  const float maxu = group_max_nan_f(x.g, x.red, mx, nan);
   // NaN keeps every comparison false, as in the reference
-  const float thr = (float)(ctl.adapt_cutoff * ctl.adapt_cutoff * maxu);
+  const float thr = cf.cut2 * maxu;
   df au{0.f, 0.f}, ae{0.f, 0.f};
   for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
     const float a2 = park[2 * j];
@@ -545,9 +574,9 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const rk_c
       ae = df_add(ae, park[2 * j + 1]);
     }
   }
-  double su = 0.0, se = 0.0;
-  group_sum2_df(x.g, x.red, au, ae, su, se);
-  return s_from_sums_f32(su, se, ctl, q);
+  df su, se;
+  group_sum2_dff(x.g, x.red, au, ae, su, se);
+  return s_from_sums_f32_fast(su, se, cf.log2_eps2, cf.safety, q);
 }
 
 // ---------------------------------------------------------------------------------
@@ -594,7 +623,7 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
     return cmul(x.c(C35_A75, j), s);
   };
   if constexpr (sizeof(T) == sizeof(float)) {
-    return unew_and_s_f32(x, k7, err, ctl, 4);
+    return unew_and_s_f32(x, k7, err, x.cf, 4);
   } else {
     double mx = write_unew(x, k7);
     return controller_s(x, mx, err, ctl, 4);
@@ -852,6 +881,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.red = red;
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
+  x.cf = make_ctlf(b.ctl);
   const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
   const rk_controller ctl = b.ctl;
 

@@ -131,18 +131,66 @@ def kdv_multi_soliton(x: np.ndarray, ampl: Sequence[float], x0: Sequence[float],
 # nonlinearity a device-side torch callable (the solvers' callable path) that reshapes,
 # transforms back, forms i gamma |F|^2 F and transforms forward.
 # ---------------------------------------------------------------------------------------
+def _pow2(n: int) -> bool:
+    return n >= 1 and (n & (n - 1)) == 0
+
+
 class SpectralNL:
     """A nonlinearity ``g -> fwd(i gamma |F|^2 F)`` with ``F = inv(g)`` on a flattened
-    spectrum; evaluated with torch on the input's device (numpy input: on the host, returned
-    as numpy)."""
+    spectrum.  On a CUDA tensor it runs the library's kernels (``_device``: line FFTs with
+    the product fused between them, ``rk_nls_lines``, and the Hankel product ``rk_dht``)
+    when the transform lengths are powers of two, torch's FFTs otherwise; NumPy input is
+    evaluated on the host and returned as NumPy."""
 
-    def __init__(self, shape, inv, fwd, gamma: float, name: str):
+    def __init__(self, shape, inv, fwd, gamma: float, name: str, ht=None):
         self.shape, self._inv, self._fwd = tuple(shape), inv, fwd
         self.gamma, self.name = float(gamma), name
+        self._ht = ht
+
+    def _lines(self, mode, n, lines, es, ls, x, out):
+        from . import _native as nat
+        from .engine import twiddles
+
+        prec = nat.RK_FP64 if x.dtype == torch.complex128 else nat.RK_FP32
+        lib = nat.load()
+        nat.check(lib.rk_nls_lines(prec, mode, n, lines, es, ls, self.gamma, x.data_ptr(), out.data_ptr(),
+                                   twiddles(x.device, prec).data_ptr(), torch.cuda.current_stream(x.device).cuda_stream),
+                  "rk_nls_lines")
+        return out
+
+    def _device(self, g):
+        """The nonlinearity on the library's kernels, or None when a length is unsupported."""
+        if g.dtype not in (torch.complex128, torch.complex64):
+            return None
+        if self.name == "nls_2d":
+            nx, ny = self.shape
+            if not (_pow2(nx) and _pow2(ny) and nx > 1 and ny > 1):
+                return None
+            G = g.reshape(nx, ny).contiguous()
+            W = torch.empty_like(G)
+            with torch.cuda.device(g.device):
+                self._lines(0, ny, nx, 1, ny, G, W)   # ifft along axis 1 (rows)
+                self._lines(2, nx, ny, ny, 1, W, W)   # fft(i gamma |v|^2 v), v = ifft, along axis 0
+                self._lines(1, ny, nx, 1, ny, W, G)   # fft along axis 1
+            return G.reshape(-1)
+        if self.name in ("nls_radial", "nls_radial_time") and self._ht is not None:
+            nt = self.shape[1] if self.name == "nls_radial_time" else 1
+            if not _pow2(nt):
+                return None
+            nr = self.shape[0]
+            X = self._ht.iht(g.reshape(nr, nt) if nt > 1 else g.reshape(nr).contiguous())
+            with torch.cuda.device(g.device):
+                self._lines(2, nt, nr, 1, nt, X, X)
+            return self._ht.ht(X).reshape(-1)
+        return None
 
     def __call__(self, g):
         if not isinstance(g, torch.Tensor):
             return self(torch.from_numpy(np.asarray(g, dtype=np.complex128))).numpy()
+        if g.is_cuda:
+            out = self._device(g)
+            if out is not None:
+                return out
         F = self._inv(g.reshape(self.shape))
         a2 = F.real * F.real + F.imag * F.imag
         return self._fwd((1j * self.gamma) * (a2 * F)).reshape(-1)
@@ -155,7 +203,7 @@ def nls_radial_ops(ht, gamma: float = 2.0) -> Tuple[np.ndarray, SpectralNL]:
     """Radially symmetric NLS on a Hankel grid (demos/nls.ipynb cells 6-12):
     L = -i kr^2, N(g) = i gamma ht(|f|^2 f) with f = iht(g); ``ht`` a
     ``transforms.HankelTransform`` (its transform runs as a GEMM on the device)."""
-    return -1j * ht.kr**2, SpectralNL((ht.nr,), ht.iht, ht.ht, gamma, "nls_radial")
+    return -1j * ht.kr**2, SpectralNL((ht.nr,), ht.iht, ht.ht, gamma, "nls_radial", ht=ht)
 
 
 def nls_radial_time_ops(ht, omega: np.ndarray, sigma: float = 0.5,
@@ -172,7 +220,7 @@ def nls_radial_time_ops(ht, omega: np.ndarray, sigma: float = 0.5,
 
     def fwd(F):
         return torch.fft.fft(ht.ht(F), dim=1)
-    return L, SpectralNL((ht.nr, len(omega)), inv, fwd, gamma, "nls_radial_time")
+    return L, SpectralNL((ht.nr, len(omega)), inv, fwd, gamma, "nls_radial_time", ht=ht)
 
 
 def nls_2d_ops(kx: np.ndarray, ky: np.ndarray, gamma: float = 2.0) -> Tuple[np.ndarray, SpectralNL]:

@@ -4,10 +4,10 @@ usable on host arrays and on device tensors.
 On the grids of ``grids.construct_r_kr_hankel`` the transform is one real matrix
 Y_ij = 2 J0(j_i j_j / j_{N+1}) / (j_{N+1} J1(j_j)^2) (J0, J1 Bessel functions of the first
 kind, j_i the zeros of J0): ``ht(f) = S Y f`` and ``iht(g) = Y g / S`` with
-S = rmax^2 / j_{N+1}.  For a torch tensor the product is a GEMM on the tensor's device over
-axis 0 (the radial axis), the real and imaginary parts of a complex tensor as one real
-matrix of 2x the columns; the matrix is built once in FP64 on the host and cached per
-device and dtype.
+S = rmax^2 / j_{N+1}.  For a CUDA tensor the product runs in the library's tiled kernel
+(``rk_dht``) over axis 0 (the radial axis), the real and imaginary parts of a complex tensor
+as one real matrix of 2x the columns; the matrix is built once in FP64 on the host and
+cached per device and dtype.  Host arrays use NumPy, as the reference does.
 """
 
 from __future__ import annotations
@@ -24,7 +24,7 @@ class HankelTransform:
     """Discrete Hankel transform on ``nr`` radial points in (0, rmax] (rkstiff/transforms.py:43)."""
 
     def __init__(self, nr: int, rmax: float = 1.0):
-        self._dev: Dict[Tuple[str, torch.dtype], Tuple[torch.Tensor, torch.Tensor]] = {}
+        self._dev: Dict[Tuple[str, torch.dtype], torch.Tensor] = {}
         self._set(nr, rmax)
 
     def _set(self, nr: int, rmax: float) -> None:
@@ -68,33 +68,46 @@ class HankelTransform:
         self._set(self._nr, rmax)
 
     # -- transforms ---------------------------------------------------------------------
-    def _matrices(self, like: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor]:
+    def _matrix(self, like: torch.Tensor) -> torch.Tensor:
         rdt = like.real.dtype if like.is_complex() else like.dtype
         key = (str(like.device), rdt)
         if key not in self._dev:
-            s = self._scalefactor()
-            fwd = torch.as_tensor(s * self._Y, dtype=torch.float64).to(device=like.device, dtype=rdt)
-            inv = torch.as_tensor(self._Y / s, dtype=torch.float64).to(device=like.device, dtype=rdt)
-            self._dev[key] = (fwd.contiguous(), inv.contiguous())
+            self._dev[key] = torch.as_tensor(self._Y, dtype=torch.float64).to(device=like.device, dtype=rdt).contiguous()
         return self._dev[key]
 
-    @staticmethod
-    def _apply(M: torch.Tensor, f: torch.Tensor) -> torch.Tensor:
-        if not f.is_complex():
-            return M @ f
-        shape = f.shape
-        fr = torch.view_as_real(f.contiguous()).reshape(shape[0], -1)  # [nr, 2 * rest]
-        out = (M @ fr).reshape(*shape, 2)
-        return torch.view_as_complex(out.contiguous())
+    def _apply(self, f: torch.Tensor, divide: bool) -> torch.Tensor:
+        if f.shape[0] != self._nr:
+            raise ValueError(f"the radial axis has {f.shape[0]} points, the transform {self._nr}")
+        if not f.is_cuda:
+            M = torch.as_tensor(self._Y / self._scalefactor() if divide else self._scalefactor() * self._Y,
+                                dtype=f.real.dtype if f.is_complex() else f.dtype)
+            if not f.is_complex():
+                return M @ f
+            fr = torch.view_as_real(f.contiguous()).reshape(f.shape[0], -1)
+            return torch.view_as_complex((M @ fr).reshape(*f.shape, 2).contiguous())
+        from . import _native as nat
+
+        if f.dtype not in (torch.float64, torch.float32, torch.complex128, torch.complex64):
+            f = f.to(torch.float64)
+        f = f.contiguous()
+        prec = nat.RK_FP64 if f.dtype in (torch.float64, torch.complex128) else nat.RK_FP32
+        w = (f.numel() // self._nr) * (2 if f.is_complex() else 1)
+        out = torch.empty_like(f)
+        lib = nat.load()
+        with torch.cuda.device(f.device):
+            nat.check(lib.rk_dht(prec, 1 if divide else 0, self._nr, w, self._matrix(f).data_ptr(),
+                                 float(self._scalefactor()), f.data_ptr(), out.data_ptr(),
+                                 torch.cuda.current_stream(f.device).cuda_stream), "rk_dht")
+        return out
 
     def ht(self, f):
         """Forward transform over axis 0: S Y f (rkstiff/transforms.py:178-208)."""
         if isinstance(f, torch.Tensor):
-            return self._apply(self._matrices(f)[0], f)
+            return self._apply(f, False)
         return self._scalefactor() * self._Y.dot(f)
 
     def iht(self, g):
         """Inverse transform over axis 0: Y g / S (rkstiff/transforms.py:210-240)."""
         if isinstance(g, torch.Tensor):
-            return self._apply(self._matrices(g)[1], g)
+            return self._apply(g, True)
         return self._Y.dot(g) / self._scalefactor()

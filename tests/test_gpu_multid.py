@@ -58,3 +58,47 @@ def test_nls_2d_fft2(golden, precision, tol):
     if precision == "fp64":
         np.testing.assert_allclose(s.t, g["nls2d_t"], rtol=1e-10)
     assert rel(uf, g["nls2d_final"]) < tol
+
+
+def _torch_eval(nl, g):
+    F = nl._inv(g.reshape(nl.shape))
+    a2 = F.real * F.real + F.imag * F.imag
+    return nl._fwd((1j * nl.gamma) * (a2 * F)).reshape(-1)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex128, 1e-13), (torch.complex64, 2e-6)])
+def test_multid_kernels_match_the_torch_composition(dtype, tol):
+    """The library's line-FFT / Hankel kernels against torch's FFTs and matrix product for
+    the three demo nonlinearities (random spectra; FP64 to rounding, FP32 to a few ulps of
+    the transform sizes)."""
+    rng = np.random.default_rng(4)
+    _, kx = construct_x_kx_fft(32, -6, 6)
+    _, ky = construct_x_kx_fft(64, -8, 8)
+    ht = HankelTransform(nr=24, rmax=4.0)
+    _, om = construct_x_kx_fft(32, -6, 6)
+    for L, nl in (models.nls_2d_ops(kx, ky, 2.0), models.nls_radial_ops(ht, 2.0),
+                  models.nls_radial_time_ops(ht, om, 0.5, 2.0)):
+        n = int(np.prod(nl.shape))
+        g = torch.as_tensor(rng.standard_normal(n) + 1j * rng.standard_normal(n), device="cuda").to(dtype)
+        dev = nl._device(g)
+        assert dev is not None, nl.name
+        ref = _torch_eval(nl, g) if dtype == torch.complex128 else \
+            _torch_eval(nl, g.to(torch.complex128)).to(dtype)
+        err = float(torch.linalg.norm(dev - ref) / torch.linalg.norm(ref))
+        assert err < tol, (nl.name, err)
+        assert torch.equal(nl(g), dev)
+
+
+def test_hankel_kernel_matches_host_product():
+    """rk_dht (device) against the NumPy product of the reference's form, S Y f and Y g / S,
+    on real and complex, 1-D and 2-D inputs."""
+    rng = np.random.default_rng(9)
+    ht = HankelTransform(nr=40, rmax=3.0)
+    for shape in ((40,), (40, 7)):
+        for cplx in (False, True):
+            f = rng.standard_normal(shape) + (1j * rng.standard_normal(shape) if cplx else 0.0)
+            ft = torch.as_tensor(f, device="cuda")
+            for fn in (ht.ht, ht.iht):
+                got = fn(ft).cpu().numpy()
+                ref = fn(f)
+                assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-13

@@ -26,9 +26,13 @@ def _config1():
 
 
 def test_config1_every_step_streamed_in_one_launch():
+    """Every accepted step's snapshot of config 1 (567 attempts) streamed in one launch:
+    the same times and states, bit for bit, as the buffered path run in one launch (a device
+    buffer of 1024 snapshots)."""
     lin, nl, u0 = _config1()
-    a = rk.IF34(lin, nl)
+    a = rk.IF34(lin, nl, device_options=rk.DeviceOptions(snap_cap=1024))
     ua = a.evolve(u0, 0.0, 50.0, store_freq=1)
+    assert a._engine().ens.launches == 1
     b = rk.IF34(lin, nl, device_options=rk.DeviceOptions(stream_snapshots=True))
     ub = b.evolve(u0, 0.0, 50.0, store_freq=1)
     assert b._engine().ens.launches == 1
