@@ -179,7 +179,19 @@ typedef struct rk_batch {
   int32_t ring_timeout_ms;
   unsigned long long* ring_head; /* [mapped host] slots claimed by the kernels            */
   const int64_t* ring_tail;      /* [mapped host] slots taken by the host                 */
+  /* Coefficient cache: 0 or 1 keeps one coefficient block per instance, rebuilt whenever h
+   * changes (the reference's exact-compare cache, etd35.py:851); 2..RK_COEF_BLOCKS_MAX keeps
+   * that many blocks keyed by their exact h (adaptive methods; the slab must then hold
+   * rk_slab_bytes_blocks(..., coef_blocks) bytes per instance; placement RK_PLACE_SMEM_ALL
+   * keeps one block).  ladder = 1 (adaptive methods with the learned controller only) puts
+   * every step size proposed after the first on the geometric ladder h0 * 2^(k/16) (h0: the
+   * instance's first step size): the nearest rung after an accepted attempt, the rung below
+   * after a rejection, so a cached block serves every return to a rung. */
+  int32_t coef_blocks;
+  int32_t ladder;
 } rk_batch;
+
+#define RK_COEF_BLOCKS_MAX 4
 
 #define RK_RING_HEADER 32
 
@@ -236,6 +248,8 @@ int rk_fill_twiddles(void* tw64, void* tw32, void* stream);
  * Replaces the coefficient / stage arrays the reference allocates per solver object
  * (e.g. rkstiff/etd35.py:129-155). */
 int64_t rk_slab_bytes(int32_t method, int32_t precision, int32_t coef_complex, int64_t m);
+/* The same with `blocks` coefficient blocks (rk_batch.coef_blocks, 1..RK_COEF_BLOCKS_MAX). */
+int64_t rk_slab_bytes_blocks(int32_t method, int32_t precision, int32_t coef_complex, int64_t m, int32_t blocks);
 
 /* Coefficient arrays of `method` at step h for a diagonal operator, FP64 math stored in
  * `precision`: the diagonal update_coeffs routines rkstiff/etd35.py:169-288,

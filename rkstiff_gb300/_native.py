@@ -61,6 +61,7 @@ class RkBatch(ctypes.Structure):
         ("mlp", ctypes.c_void_p),
         ("ring_data", ctypes.c_void_p), ("ring_slot_bytes", ctypes.c_int64), ("ring_slots", ctypes.c_int32),
         ("ring_timeout_ms", ctypes.c_int32), ("ring_head", ctypes.c_void_p), ("ring_tail", ctypes.c_void_p),
+        ("coef_blocks", ctypes.c_int32), ("ladder", ctypes.c_int32),
     ]
 
 
@@ -117,7 +118,8 @@ STATE_DTYPE = np.dtype([
 assert STATE_DTYPE.itemsize == 128
 
 # every symbol the header declares
-EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_num_coeffs", "rk_coeffs",
+EXPORTS = ("rk_abi_version", "rk_last_error", "rk_fill_twiddles", "rk_slab_bytes", "rk_slab_bytes_blocks",
+           "rk_num_coeffs", "rk_coeffs",
            "rk_evolve", "rk_probe_fp32", "rk_evolve_noalloc", "rk_mlp_forward", "rk_mlp_grad", "rk_mlp_adam",
            "rk_mlp_pack", "rk_dense_work_bytes", "rk_dense_evolve", "rk_tf32x3_work_bytes", "rk_tf32x3_gemm",
            "rk_combine", "rk_error_s", "rk_cgemv", "rk_dense_eig_work_bytes", "rk_dense_eig_evolve",
@@ -153,6 +155,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         lib.rk_fill_twiddles.restype = ctypes.c_int
         lib.rk_slab_bytes.argtypes = [i32, i32, i32, i64]
         lib.rk_slab_bytes.restype = i64
+        lib.rk_slab_bytes_blocks.argtypes = [i32, i32, i32, i64, i32]
+        lib.rk_slab_bytes_blocks.restype = i64
         lib.rk_num_coeffs.argtypes = [i32]
         lib.rk_num_coeffs.restype = ctypes.c_int
         lib.rk_coeffs.argtypes = [i32, i32, i32, i64, vp, dbl, ctypes.POINTER(RkEtdConfig), vp, vp]

@@ -86,11 +86,11 @@ def collect_logs(ensemble, u0s, t0: float, tf: float, cap: int = 4096, h_init: O
     eng = ensemble.engine
     eng.attempt_log = torch.zeros((eng.n_inst, cap, nat.RK_LOG_FIELDS), dtype=torch.float32, device=eng.device)
     eng.log_cap = cap
-    mlp, target = eng.mlp, eng.mlp_target
+    mlp, target, cache = eng.mlp, eng.mlp_target, (eng.coef_blocks, eng.ladder)
     if controller is None:
         eng.mlp = None
     else:
-        controller.install(ensemble)
+        controller.install(ensemble, ladder=False)  # the logs the shipped network was trained on
     try:
         try:
             ensemble.evolve(u0s, t0, tf, h_init, max_steps=max_steps, max_launches=max_launches)
@@ -101,6 +101,7 @@ def collect_logs(ensemble, u0s, t0: float, tf: float, cap: int = 4096, h_init: O
         eng.attempt_log = None
         eng.log_cap = 0
         eng.mlp, eng.mlp_target = mlp, target
+        eng.set_coef_cache(cache[0], ladder=bool(cache[1]))
     return log, ensemble.stats()["attempts"]
 
 
@@ -216,10 +217,16 @@ class LearnedController:
             self._packed = out
         return self._packed
 
-    def install(self, ensemble) -> None:
-        """Make ``ensemble`` use this controller on accepted attempts."""
+    def install(self, ensemble, ladder: bool = False) -> None:
+        """Make ``ensemble`` use this controller on accepted attempts.  With ``ladder`` its
+        step sizes are put on the geometric ladder h0 2^(k/16) (the rung nearest the
+        proposal; after a rejection the rung below) and each instance keeps four
+        coefficient blocks keyed by h, so a return to a recent rung rebuilds nothing (the
+        network changes h on most accepted steps, where the reference's single-entry cache
+        rebuilds the coefficients every attempt)."""
         ensemble.engine.mlp = self.packed()
         ensemble.engine.mlp_target = self.target
+        ensemble.engine.set_coef_cache(4 if ladder else 1, ladder=ladder)
 
     def save(self, path: str) -> None:
         """Parameters, input normalisation and target as a .npz file."""

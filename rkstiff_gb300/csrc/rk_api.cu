@@ -216,6 +216,10 @@ int validate_batch(const rk_batch* b, bool need_scratch) {
     set_error("rk_evolve: unknown placement");
     return RK_E_ARG;
   }
+  if (b->coef_blocks < 0 || b->coef_blocks > RK_COEF_BLOCKS_MAX || b->ladder < 0 || b->ladder > 1) {
+    set_error("rk_evolve: coef_blocks must be in [0, RK_COEF_BLOCKS_MAX] and ladder 0 or 1");
+    return RK_E_ARG;
+  }
   return RK_OK;
 }
 
@@ -238,6 +242,11 @@ int rk_fill_twiddles(void* tw64, void* tw32, void* stream) {
 int64_t rk_slab_bytes(int32_t method, int32_t precision, int32_t coef_complex, int64_t m) {
   if (check_method(method) || m <= 0) return -1;
   return slab_bytes(method, precision, coef_complex, m);
+}
+
+int64_t rk_slab_bytes_blocks(int32_t method, int32_t precision, int32_t coef_complex, int64_t m, int32_t blocks) {
+  if (check_method(method) || m <= 0 || blocks < 1 || blocks > RK_COEF_BLOCKS_MAX) return -1;
+  return slab_bytes(method, precision, coef_complex, m, blocks);
 }
 
 int rk_num_coeffs(int32_t method) {

@@ -50,13 +50,33 @@ RK_HD int traits_nv(int method) { return traits_nn(method) + (unew_in_n2(method)
 // bytes of an instance's scratch: u, unew, N1..NN (complex T), the coefficient block and,
 // in FP32, a working-precision copy of the wavenumbers (read once per nonlinear evaluation
 // per mode; converting the FP64 input there would put a conversion per mode on the FP64 pipe)
-RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m) {
+RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m, int blocks = 1) {
   const int64_t mp = round_up4(m);
   const int64_t ts = precision == RK_FP64 ? 8 : 4;
   const int64_t vec = 2 * ts * mp;
   const int64_t coef = (coef_complex ? 2 : 1) * ts * mp;
   const int64_t kxw = precision == RK_FP64 ? 0 : ts * mp;
-  return traits_nv(method) * vec + num_coeffs(method) * coef + kxw;
+  // with several coefficient blocks: the extra blocks, then their h tags
+  const int64_t extra = blocks > 1 ? (blocks - 1) * num_coeffs(method) * coef + 8 * RK_COEF_BLOCKS_MAX : 0;
+  return traits_nv(method) * vec + num_coeffs(method) * coef + kxw + extra;
+}
+
+// 2^(r/16), r = 0..15: the rungs of the learned controller's step-size ladder within an octave
+__constant__ const double k_ladder[16] = {
+    1.0, 1.0442737824274138, 1.0905077326652577, 1.1387886347566916, 1.189207115002721, 1.241857812073484,
+    1.2968395546510096, 1.3542555469368927, 1.4142135623730951, 1.4768261459394993, 1.5422108254079407,
+    1.6104903319492543, 1.681792830507429, 1.7562521603732995, 1.8340080864093424, 1.9152065613971474};
+
+RK_DEV double ladder_rung(double h0, int k) { return h0 * k_ladder[k & 15] * ldexp(1.0, k >> 4); }
+
+// the rung h0 * 2^(k/16) (k an integer) nearest to h, or (floor) the largest not above h;
+// the rung is picked in FP32, the floor checked in FP64
+RK_DEV double ladder_step(double h, double h0, bool floor_) {
+  const float l = 16.f * log2f((float)(h / h0));
+  int k = floor_ ? (int)floorf(l + 1e-3f) : (int)rintf(l);
+  double v = ladder_rung(h0, k);
+  if (floor_ && v > h) v = ladder_rung(h0, --k);
+  return v;
 }
 
 // FP32 controller constants, formed once per instance run so that no attempt needs FP64
@@ -875,7 +895,10 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.u = ssl;
   for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + ((U2 ? 1 : 2) + i) * x.mp : nullptr;
   x.unew = U2 ? x.N[1] : ssl + x.mp;
-  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NV * x.mp) : reinterpret_cast<CT*>(gsl + NV * x.mp);
+  // global slab: [NV vectors | FP32 wavenumbers | coefficient block(s) | block tags]
+  constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
+  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NV * x.mp)
+                             : reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NV * x.mp) + KXW * x.mp);
   x.fa = fa;
   x.fb = fb;
   x.red = red;
@@ -906,7 +929,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     } else {
       // FP32: a working-precision copy after the coefficient block (shared memory when the
       // stage arrays are there, the global slab otherwise), filled once per launch
-      T* kw = PLACE == PL_GLOBAL ? reinterpret_cast<T*>(reinterpret_cast<CT*>(gsl + NV * x.mp) + Tr::NC * x.mp)
+      T* kw = PLACE == PL_GLOBAL ? reinterpret_cast<T*>(gsl + NV * x.mp)
             : PLACE == PL_SMEM_STATE ? reinterpret_cast<T*>(ssl + NV * x.mp)
                                      : reinterpret_cast<T*>(x.C + Tr::NC * x.mp);
       const double* kd = b.kx + mo;
@@ -920,6 +943,35 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
 
   double t = st.t, tf = st.tf, h = st.h;
   double hc = PLACE == PL_SMEM_ALL ? nan_d() : st.h_coeff;
+  // Coefficient blocks (b.coef_blocks > 1): block i at C0 + i * blk, its h tag in the slab
+  // after the blocks (tags[i], persistent across launches).  A stale record (h_coeff NaN:
+  // fresh state, or a noalloc call) invalidates every tag.
+  const int nblk =
+      (!Tr::ADAPT || PLACE == PL_SMEM_ALL || b.coef_blocks <= 1) ? 1 : min(b.coef_blocks, RK_COEF_BLOCKS_MAX);
+  CT* const C0 = x.C;
+  const int64_t blk = (int64_t)Tr::NC * x.mp;
+  double* tags = nblk > 1 ? reinterpret_cast<double*>(
+                                reinterpret_cast<unsigned char*>(gsl) +
+                                (slab_bytes(METHOD, sizeof(T) == 8 ? RK_FP64 : RK_FP32, sizeof(CT) == 2 * sizeof(T), x.m,
+                                            nblk) - 8 * RK_COEF_BLOCKS_MAX))
+                          : nullptr;
+  int victim = 0;
+  if (nblk > 1) {
+    if (hc != hc) {
+      if (g.tid < RK_COEF_BLOCKS_MAX) tags[g.tid] = nan_d();
+      g.sync();
+    } else {
+      int found = -1;
+      for (int i = 0; i < nblk; ++i)
+        if (tags[i] == hc) found = i;
+      if (found >= 0) x.C = C0 + found * blk;
+      else hc = nan_d();  // no block holds h_coeff: rebuild before the first attempt
+    }
+  }
+  // the learned controller's step-size ladder starts at the instance's first step size
+  const bool ladder = Tr::ADAPT && b.ladder != 0 && b.mlp != nullptr;
+  double h0 = st.reserved_d;
+  if (ladder && (st.steps == 0 && st.attempts == 0)) h0 = st.h;
   bool accept = st.accept != 0;
   bool n1_valid = false;
   const bool resumed = st.steps > 0;
@@ -942,9 +994,21 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       double hs = h;
       for (;;) {
         if (h != hc) {  // exact compare, as the reference's _update_coeffs
-          compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+          int hit = -1;
+          for (int i = 0; i < nblk && nblk > 1; ++i)
+            if (tags[i] == h) hit = i;
+          if (hit >= 0) {
+            x.C = C0 + hit * blk;
+          } else {
+            if (nblk > 1) {
+              x.C = C0 + victim * blk;
+              if (g.tid == 0) tags[victim] = h;  // published by compute_coeffs' closing barrier
+              victim = (victim + 1) % nblk;
+            }
+            compute_coeffs<T, CT, S, METHOD>(x, h, ec);
+            ++coeff_updates;
+          }
           hc = h;
-          ++coeff_updates;
         }
         int nlc = 0;
         if (!n1_valid || (METHOD == RK_ETD35 && accept)) {
@@ -982,6 +1046,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
           ++rejects;
           h_prev = h;
           h = reject_h(s, h, ctl);
+          if (ladder) h = ladder_step(h, h0, true);  // a rejection never grows the step
           ++numloops;
           s_prev2 = s_prev;
           s_prev = f_s;
@@ -1012,6 +1077,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
             const float d = fminf(fmaxf(y, -1.f), 1.f);
             const double fac = fmin(fmax(exp((double)(f_s + d)) / (double)b.mlp_target, 0.5), 4.0);
             hs = (y == y) ? h * fac : accept_h(s, h, ctl);
+            if (ladder) hs = ladder_step(hs, h0, false);
           } else {
             hs = accept_h(s, h, ctl);
           }
@@ -1081,6 +1147,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     st.t = t;
     st.h = h;
     st.h_coeff = PLACE == PL_SMEM_ALL ? nan_d() : hc;
+    if (ladder) st.reserved_d = h0;
     st.h_used = h_used;
     st.h_suggest = h_sug;
     st.s_last = s_last;

@@ -69,7 +69,8 @@ extern "C" int rk_evolve_noalloc(const rk_batch* b, void* stream) {
   if (int e = validate_batch(b, false)) return e;
   if (b->n_inst == 0) return RK_OK;
   const int64_t m_max = (b->nl_kind == RK_NL_UUX) ? b->n_max / 2 + 1 : b->n_max;
-  const int64_t stride = (slab_bytes(b->method, b->precision, b->coef_complex, m_max) + 255) / 256 * 256;
+  const int blocks = b->coef_blocks > 1 ? b->coef_blocks : 1;
+  const int64_t stride = (slab_bytes(b->method, b->precision, b->coef_complex, m_max, blocks) + 255) / 256 * 256;
   // bound the instance count before any product: 256 bytes of counters, 8 bytes of offset
   // and one slab per instance, plus at most 255 bytes of offset-table padding
   const int64_t avail = (int64_t)RK_NOALLOC_SCRATCH_BYTES - 256 - 255;
@@ -119,8 +120,8 @@ extern "C" int rk_evolve_noalloc(const rk_batch* b, void* stream) {
   b2.slab_off = offs;
   b2.slab = sc + 256 + off_bytes;
   cudaStream_t s = (cudaStream_t)stream;
-  const unsigned blocks = (unsigned)((b->n_inst + 255) / 256);
-  noalloc_prepare_kernel<<<blocks, 256, 0, s>>>(offs, b->n_inst, stride, b->state);
+  const unsigned nb = (unsigned)((b->n_inst + 255) / 256);
+  noalloc_prepare_kernel<<<nb, 256, 0, s>>>(offs, b->n_inst, stride, b->state);
   if (int e = cuda_check(cudaGetLastError(), "noalloc prepare launch")) return e;
   return rk_evolve(&b2, stream);
 }

@@ -152,15 +152,9 @@ class DiagEnsemble:
         self.class_threads = None  # per-class threads (np.int32) or None: library default
         self.class_place = None    # per-class placement (np.int32) or None: library default
         self.class_groups = None   # per-class instance groups per block (np.int32) or None
-        sizes = [int(self.lib.rk_slab_bytes(self.method, self.prec, self.coef_complex, int(m))) for m in ms]
-        offs = np.zeros(n_inst, dtype=np.int64)
-        acc = 0
-        for i, s in enumerate(sizes):
-            offs[i] = acc
-            acc += (s + 255) // 256 * 256
-        self.slab_bytes = acc
-        self.slab = torch.empty(max(acc, 256), dtype=torch.uint8, device=dev)
-        self.slab_off_dev = torch.from_numpy(offs).to(dev)
+        self.coef_blocks = 1
+        self.ladder = 0
+        self._alloc_slab()
         self.state_dev = torch.zeros(n_inst * nat.STATE_DTYPE.itemsize, dtype=torch.uint8, device=dev)
         self.queue = torch.zeros(max(1, len(self.class_n)), dtype=torch.int32, device=dev)
         self.tw = twiddles(dev, self.prec)
@@ -174,6 +168,31 @@ class DiagEnsemble:
         self.log_cap = 0
         self.mlp = None             # packed learned-controller buffer (uint8 device tensor) or None
         self.mlp_target = 1.25
+
+    def _alloc_slab(self) -> None:
+        sizes = [int(self.lib.rk_slab_bytes_blocks(self.method, self.prec, self.coef_complex, int(m),
+                                                   int(self.coef_blocks))) for m in self.ms]
+        offs = np.zeros(self.n_inst, dtype=np.int64)
+        acc = 0
+        for i, sz in enumerate(sizes):
+            offs[i] = acc
+            acc += (sz + 255) // 256 * 256
+        self.slab_bytes = acc
+        self.slab = torch.empty(max(acc, 256), dtype=torch.uint8, device=self.device)
+        self.slab_off_dev = torch.from_numpy(offs).to(self.device)
+
+    def set_coef_cache(self, blocks: int, ladder: bool = False) -> None:
+        """Keep ``blocks`` coefficient blocks per instance keyed by their exact h (1: the
+        reference's single-entry cache) and, with ``ladder``, put the learned controller's
+        step sizes on the 2^(1/16) ladder (rk_batch.coef_blocks / ladder); a change of
+        ``blocks`` reallocates the scratch, so the next launch rebuilds the coefficients."""
+        blocks = int(blocks)
+        if not 1 <= blocks <= 4:
+            raise ValueError("blocks must be in 1..4")
+        if blocks != self.coef_blocks:
+            self.coef_blocks = blocks
+            self._alloc_slab()
+        self.ladder = 1 if ladder else 0
 
     # -- configuration ----------------------------------------------------------------
     def set_config(self, config=None, etd_config=None):
@@ -271,6 +290,8 @@ class DiagEnsemble:
         b.mlp_target = float(self.mlp_target)
         if ring is not None:
             ring.fill_batch(b)
+        b.coef_blocks = int(self.coef_blocks)
+        b.ladder = int(self.ladder)
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device)
             if self.record_events:
@@ -293,6 +314,7 @@ class DiagEnsemble:
                tuple(int(v) for v in (self.class_groups if self.class_groups is not None else ())),
                tuple(int(v) for v in (self.class_place if self.class_place is not None else ())),
                None if self.mlp is None else self.mlp.data_ptr(), float(self.mlp_target),
+               int(self.coef_blocks), int(self.ladder), self.slab.data_ptr(),
                None if self.attempt_log is None else self.attempt_log.data_ptr())
         if getattr(self, "_graph_key", None) != key:
             fresh = torch.from_numpy(np.ascontiguousarray(self.fresh_state(t0, tf, h)).view(np.uint8)).to(self.device)

@@ -166,13 +166,14 @@ class SpectralNL:
             nx, ny = self.shape
             if not (_pow2(nx) and _pow2(ny) and nx > 1 and ny > 1):
                 return None
-            G = g.reshape(nx, ny).contiguous()
+            G = g.reshape(nx, ny).contiguous()  # may be a view of the caller's tensor: read only
             W = torch.empty_like(G)
+            out = torch.empty_like(G)
             with torch.cuda.device(g.device):
                 self._lines(0, ny, nx, 1, ny, G, W)   # ifft along axis 1 (rows)
                 self._lines(2, nx, ny, ny, 1, W, W)   # fft(i gamma |v|^2 v), v = ifft, along axis 0
-                self._lines(1, ny, nx, 1, ny, W, G)   # fft along axis 1
-            return G.reshape(-1)
+                self._lines(1, ny, nx, 1, ny, W, out)  # fft along axis 1
+            return out.reshape(-1)
         if self.name in ("nls_radial", "nls_radial_time") and self._ht is not None:
             nt = self.shape[1] if self.name == "nls_radial_time" else 1
             if not _pow2(nt):

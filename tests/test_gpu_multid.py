@@ -80,8 +80,10 @@ def test_multid_kernels_match_the_torch_composition(dtype, tol):
                   models.nls_radial_time_ops(ht, om, 0.5, 2.0)):
         n = int(np.prod(nl.shape))
         g = torch.as_tensor(rng.standard_normal(n) + 1j * rng.standard_normal(n), device="cuda").to(dtype)
+        g0 = g.clone()
         dev = nl._device(g)
         assert dev is not None, nl.name
+        assert torch.equal(g, g0), nl.name  # the input is left as it was
         ref = _torch_eval(nl, g) if dtype == torch.complex128 else \
             _torch_eval(nl, g.to(torch.complex128)).to(dtype)
         err = float(torch.linalg.norm(dev - ref) / torch.linalg.norm(ref))
