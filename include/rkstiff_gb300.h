@@ -81,12 +81,19 @@ typedef struct rk_controller {
   double epsilon, incr_f, decr_f, safety_f, adapt_cutoff, minh;
 } rk_controller;
 
-/* psi-function settings: ETDConfig, rkstiff/etd.py:46-131 */
+/* psi-function settings: ETDConfig, rkstiff/etd.py:46-131.  contour_at_zero = 1 evaluates
+ * every mode's psi values as the reference's non-diagonal strategies do for a matrix
+ * operator: the mean over the contour nodes r_j (radius contour_radius, centred at 0) of
+ * r_j psi(r_j) / (r_j - c z) for each scaled argument c z (etd35.py:602-658,
+ * etd34.py:366-383, etd4.py:245-262, etd5.py); applied to the eigenvalues of a
+ * diagonalizable lin_op this reproduces the reference's psi-matrices
+ * S diag(.) S^-1.  0: the diagonal rule (direct formula, contour around z below
+ * modecutoff). */
 typedef struct rk_etd_config {
   double modecutoff;
   double contour_radius;
   int32_t contour_points;
-  int32_t reserved;
+  int32_t contour_at_zero;
 } rk_etd_config;
 
 /* per-instance controller state (the attributes rkstiff keeps on the solver object:

@@ -62,6 +62,7 @@ class CallableBackend:
         self._cptr = [self.C[c * self.m:(c + 1) * self.m].data_ptr() for c in range(ncoef)]
         self.s_dev = torch.zeros(1, dtype=torch.float64, device=self.device)
         self.adaptive = method in Q
+        self._contour_at_zero = False  # the eigenbasis backend may take the reference's matrix contour
         self.reset()
 
     # -- bookkeeping ------------------------------------------------------------------
@@ -81,8 +82,9 @@ class CallableBackend:
         if h == self.hc:  # exact compare, etd35.py:851
             return
         e = getattr(self.solver, "etd_config", None)
-        etd = nat.RkEtdConfig(e.modecutoff, e.contour_radius, e.contour_points, 0) if e is not None else \
-            nat.RkEtdConfig(0.01, 1.0, 32, 0)
+        zero = 1 if self._contour_at_zero else 0
+        etd = nat.RkEtdConfig(e.modecutoff, e.contour_radius, e.contour_points, zero) if e is not None else \
+            nat.RkEtdConfig(0.01, 1.0, 32, zero)
         nat.check(self.lib.rk_coeffs(self.method, self.prec, self.coef_complex, self.m, self.lin_dev.data_ptr(), h,
                                      ctypes.byref(etd), self.C.data_ptr(), self._stream()), "rk_coeffs")
         self.hc = h
@@ -293,6 +295,12 @@ class EigenBackend(CallableBackend):
         self.Sinv = torch.as_tensor(np.ascontiguousarray(Sinv, dtype=np.complex128), device=self.device).to(
             self.cdtype)
         self.err_physical = not diagonalize
+        dense_psi = getattr(solver.device_options, "dense_psi", "exact")
+        if dense_psi not in ("exact", "contour"):
+            raise ValueError("dense_psi must be 'exact' or 'contour'")
+        # the reference's non-diagonal psi-matrices (a zero-centred contour of resolvents);
+        # the diagonalized strategy uses the diagonal rule, as the reference's does
+        self._contour_at_zero = dense_psi == "contour" and not diagonalize
 
     def _mv(self, M, x):
         y = torch.empty(self.n, dtype=self.cdtype, device=self.device)

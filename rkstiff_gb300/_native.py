@@ -38,7 +38,7 @@ class RkController(ctypes.Structure):
 
 class RkEtdConfig(ctypes.Structure):
     _fields_ = [("modecutoff", ctypes.c_double), ("contour_radius", ctypes.c_double),
-                ("contour_points", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("contour_points", ctypes.c_int32), ("contour_at_zero", ctypes.c_int32)]
 
 
 class RkBatch(ctypes.Structure):

@@ -326,6 +326,46 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
+  if (ec.zero) {
+    // the reference's matrix form on each mode: warp per mode, lanes over the nodes r_q,
+    // summands r_q psi_k(r_q) / (r_q - c z) (psi of the node, the resolvent of the scaled z)
+    const int lane = g.tid & 31, warp = g.tid >> 5, nwarp = g.nthr >> 5;
+    for (int j = warp; j < m; j += nwarp) {
+      S z = load_z<S>(lin, j, h);
+      const cx<double> zc = to_cx(z);
+      cx<double> acc[NP];
+#pragma unroll
+      for (int k = 0; k < NP; ++k) acc[k] = cx<double>{0.0, 0.0};
+      for (int q = lane; q < ec.np; q += 32) {
+        const cx<double> r = contour_node(ec, q);
+        const cx<double> e = cexp(r);
+        const cx<double> p1 = psi1(r, e), p2 = psi2(r, e), p3 = psi3(r, e);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+          int order;
+          double num, den;
+          psi_slot(METHOD, k, order, num, den);
+          const cx<double> cz = (num == 1.0 && den == 1.0) ? zc : rdiv(num * zc, den);
+          const cx<double> pv = order == 1 ? p1 : (order == 2 ? p2 : p3);
+          acc[k] = acc[k] + (r * pv) * crecip(r - cz);
+        }
+      }
+      S P[NP];
+#pragma unroll
+      for (int k = 0; k < NP; ++k) {
+        double re = warp_sum(acc[k].x), im = warp_sum(acc[k].y);
+        P[k] = from_cx<S>(rdiv(h * cx<double>{re, im}, (double)ec.np));
+      }
+      if (lane == 0) {
+        S o[NC];
+        etd_from_psi<S>(METHOD, z, P, o);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+      }
+    }
+    g.sync();
+    return;
+  }
   const dd hdd = dd_from_double(h);
   // pass 1: thread per mode, direct formula for |z| >= modecutoff; with FAST the small
   // modes are evaluated here too, by the Taylor series of psi_k (see taylor_psi)
@@ -905,7 +945,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
   x.cf = make_ctlf(b.ctl);
-  const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
+  const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points, b.etd.contour_at_zero};
   const rk_controller ctl = b.ctl;
 
   rk_inst_state st = b.state[inst];
@@ -1210,7 +1250,7 @@ __global__ void coeff_kernel(int m, const double* lin, double h, rk_etd_config e
   const Group g{(int)threadIdx.x, (int)blockDim.x, 0};
   const int per = blockDim.x;
   const int j0 = blockIdx.x * per;
-  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points};
+  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points, etd.contour_at_zero};
   // arrays of length m, shifted so that c*m + j addresses mode j0 + j
   compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(g, min(per, m - j0), m,
                                                                 reinterpret_cast<const cx<double>*>(lin) + j0,

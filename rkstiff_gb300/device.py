@@ -18,6 +18,10 @@ class DeviceOptions:
     device    : CUDA device (default: the current one)
     threads   : threads per instance group (0: the kernel default, 256)
     snap_cap  : snapshots the device buffers hold before the host drains them
+    dense_psi : for a 2-D lin_op with diagonalize=False: 'exact' (default) applies the
+                psi-functions of the eigenvalues; 'contour' reproduces the reference's own
+                psi-matrices, its mean of r psi(r) (rI - cZ)^-1 over a contour centred at 0
+                (etd35.py:602-658), whose error grows with |h eig| beyond the radius
     stream_snapshots : stream the snapshots of evolve through a pinned, mapped host ring
                 while the launch runs (one launch to tf, no device snapshot buffer)
     snapshot_file : path of an .npz file (arrays t and u) the streamed snapshots are
@@ -29,5 +33,6 @@ class DeviceOptions:
     device: Optional[Union[str, torch.device]] = None
     threads: int = 0
     snap_cap: int = 256
+    dense_psi: str = "exact"
     stream_snapshots: bool = False
     snapshot_file: Optional[str] = None

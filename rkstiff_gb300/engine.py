@@ -204,7 +204,7 @@ class DiagEnsemble:
         e = etd_config
         self.etd = nat.RkEtdConfig(modecutoff=getattr(e, "modecutoff", 0.01),
                                    contour_radius=getattr(e, "contour_radius", 1.0),
-                                   contour_points=int(getattr(e, "contour_points", 32)), reserved=0)
+                                   contour_points=int(getattr(e, "contour_points", 32)), contour_at_zero=0)
 
     # -- state records ----------------------------------------------------------------
     def fresh_state(self, t0, tf, h) -> np.ndarray:

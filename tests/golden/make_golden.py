@@ -422,6 +422,21 @@ def derivs_cases(out):
     out["dcheb_swapped"] = derivatives.dx_cheb(arr, np.eye(8))
 
 
+def if45dp_cases(out):
+    """IF45DP adaptive over a longer span than the stiff KS case allows: the KdV soliton
+    (n = 256 on [-30, 30)), epsilon = 1e-4, t in [0, 5] (~3600 accepted steps)."""
+    from rkstiff import if45dp, models, grids
+    from rkstiff.solveras import SolverConfig
+    x, kx = grids.construct_x_kx_rfft(256, -30, 30)
+    u0 = np.fft.rfft(models.kdv_soliton(x, ampl=1.0, x0=-5.0, t=0))
+    lin, nl = models.kdv_ops(kx)
+    s = if45dp.IF45DP(lin, nl, config=SolverConfig(epsilon=1e-4))
+    rec = Recorder(s)
+    out["kdv_IF45DP_final"] = s.evolve(u0, t0=0.0, tf=5.0, h_init=0.025, store_freq=100)
+    out["kdv_IF45DP_t"] = np.array(s.t)
+    out["kdv_IF45DP_s"] = np.array(rec.s)
+
+
 def multid_cases(out):
     """The multi-dimensional spectral problems of the reference's NLS demo (demos/nls.ipynb):
     the radial NLS on a Hankel grid, the (r, t) NLS with a Hankel transform in r and an FFT
@@ -491,7 +506,7 @@ def multid_cases(out):
 CASES = (("coeffs", coeff_cases), ("fixed_step", fixed_step_cases), ("adaptive", adaptive_cases),
          ("controller", controller_cases), ("dense", dense_cases), ("failure", failure_cases),
          ("multid", multid_cases), ("nls4096", nls4096_cases),
-         ("derivs", derivs_cases))
+         ("derivs", derivs_cases), ("if45dp", if45dp_cases))
 
 
 def main():

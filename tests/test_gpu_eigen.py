@@ -26,6 +26,7 @@ import torch
 
 import rkstiff_gb300 as rk
 from oracle import rk_oracle as O
+from rkstiff_gb300 import _native as nat
 from rkstiff_gb300.device import DeviceOptions
 
 pytestmark = pytest.mark.gpu
@@ -167,3 +168,54 @@ def test_fp32_dense_one_step(ac):
     ref, h_ref, _ = o.step(w0.astype(np.complex128), 0.05)
     assert h_used == h_ref
     assert rel(unew, ref) < 2e-6
+
+
+def test_reference_contour_psi_matrices(ac):
+    """rk_coeffs with contour_at_zero on the eigenvalues, transformed back (S diag(c) S^-1),
+    against the reference's own non-diagonal ETD35 matrices at h = 0.05 (contour radius 10,
+    32 points; etd35.py:602-658)."""
+    import ctypes
+
+    g, lin, _, _, _ = ac
+    lib = nat.load()
+    eig, S = np.linalg.eig(lin)
+    Sinv = np.linalg.inv(S)
+    m = eig.shape[0]
+    cfg = nat.RkEtdConfig(modecutoff=0.01, contour_radius=10.0, contour_points=32, contour_at_zero=1)
+    lin_d = torch.from_numpy(eig.astype(np.complex128)).cuda()
+    nc = lib.rk_num_coeffs(nat.RK_ETD35)
+    out = torch.zeros(nc * m, dtype=torch.complex128, device="cuda")
+    nat.check(lib.rk_coeffs(nat.RK_ETD35, nat.RK_FP64, 1, m, lin_d.data_ptr(), 0.05, ctypes.byref(cfg),
+                            out.data_ptr(), torch.cuda.current_stream().cuda_stream), "rk_coeffs")
+    C = out.cpu().numpy().reshape(nc, m)
+    order = ["E14", "E12", "E34", "EL", "a21", "a31", "a32", "a41", "a43", "a51", "a52", "a54", "a61", "a62",
+             "a63", "a65", "a71", "a73", "a74", "a75", "a76"]
+    for name in ("EL", "a21", "a54", "a65", "a76"):
+        M = (S * C[order.index(name)]) @ Sinv
+        ref = g[f"ac20_ETD35_dense_{name}"]
+        assert np.max(np.abs(M - ref)) / np.max(np.abs(ref)) < 1e-11, name
+
+
+@pytest.mark.parametrize("method,tf,key,tol", [("ETD35", 60.0, "ac20_ETD35_nondiag_final", 1e-7),
+                                               ("ETD34", 10.0, "ac20_ETD34_nondiag_final", 1e-9)])
+def test_reference_contour_mode_runs(ac, method, tf, key, tol):
+    """DeviceOptions(dense_psi='contour'): the reference's non-diagonal runs themselves (the
+    default exact-psi form is 5e-5 / 1e-4 away from them), with the oracle's attempt count."""
+    g, lin, w0, nl_t, nl_np = ac
+    cfg = rk.ETDConfig(contour_points=32, contour_radius=10)
+    s = getattr(rk, method)(lin, nl_t, config=rk.SolverConfig(epsilon=1e-4), etd_config=cfg,
+                            device_options=rk.DeviceOptions(dense_psi="contour"))
+    uf = s.evolve(w0, 0.0, tf, store_data=False)
+    o = O.OracleSolver(method, lin, nl_np, O.SolverConfig(epsilon=1e-4),
+                       O.ETDConfig(contour_points=32, contour_radius=10), dense_psi="contour")
+    o.evolve(w0.astype(np.complex128), 0.0, tf, store_data=False)
+    assert s.stats["attempts"] == o.attempts
+    assert rel(uf, g[key]) < tol
+
+
+def test_reference_contour_mode_fixed_step(ac):
+    g, lin, w0, nl_t, _ = ac
+    cfg = rk.ETDConfig(contour_points=32, contour_radius=10)
+    s = rk.ETD4(lin, nl_t, etd_config=cfg, device_options=rk.DeviceOptions(dense_psi="contour"))
+    uf = s.evolve(w0, 0.0, 2.0, 0.01, store_data=False)
+    assert rel(uf, g["ac20_ETD4_dense_final"]) < 1e-11

@@ -169,6 +169,20 @@ def test_adaptive_ks256_fp64(golden, method):
     assert rel(uf, g[f"ks256_{method}_final"]) < 1e-8
 
 
+def test_adaptive_kdv_if45dp_long_fp64(golden):
+    """IF45DP adaptive over a long span (t in [0, 5], 3627 attempts, KdV soliton) with the
+    reference's attempt count and snapshot times; the stiff KS case above stops at t = 0.5."""
+    g = golden("if45dp")
+    x, kx = rk.grids.construct_x_kx_rfft(256, -30, 30)
+    lin, nl = models.kdv_ops(kx)
+    u0 = np.fft.rfft(models.kdv_soliton(x, ampl=1.0, x0=-5.0))
+    s = rk.IF45DP(lin, nl, config=rk.SolverConfig(epsilon=1e-4))
+    uf = s.evolve(u0, 0.0, 5.0, h_init=0.025, store_freq=100)
+    assert s.stats["attempts"] == len(g["kdv_IF45DP_s"])
+    np.testing.assert_allclose(s.t, g["kdv_IF45DP_t"], rtol=1e-10)
+    assert rel(uf, g["kdv_IF45DP_final"]) < 1e-9
+
+
 def test_adaptive_nls_etd35_fp64(golden):
     g = golden("adaptive")
     x, kx = rk.grids.construct_x_kx_fft(256, -20.0, 20.0)

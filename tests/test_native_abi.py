@@ -150,7 +150,7 @@ def _fake_batch(n_inst, n_max):
     b.n_max = n_max
     for f in ("n", "mode_off", "lin_op", "kx", "u", "state", "twiddle"):
         setattr(b, f, 0x1000)
-    b.etd = nat.RkEtdConfig(modecutoff=0.01, contour_radius=1.0, contour_points=32, reserved=0)
+    b.etd = nat.RkEtdConfig(modecutoff=0.01, contour_radius=1.0, contour_points=32, contour_at_zero=0)
     return b
 
 

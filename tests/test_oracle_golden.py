@@ -319,3 +319,15 @@ def test_grids_and_derivatives(golden):
     x, D = OD.cheb_grid(20, -1, 1)
     U = np.stack([np.sin(x), np.cos(2 * x), x**3], axis=1)
     assert _close(OD.dx_cheb(D, U, 2), g["dcheb_c20_2d_2"], 1e-11)
+
+
+def test_adaptive_kdv_if45dp_long(golden):
+    """IF45DP over t in [0, 5] on the KdV soliton (3627 attempts), against the reference."""
+    g = golden("if45dp")
+    kx, lin, nl, u0 = P.kdv_problem()
+    s = O.OracleSolver("IF45DP", lin, nl, O.SolverConfig(epsilon=1e-4))
+    uf = s.evolve(u0, 0.0, 5.0, h_init=0.025, store_freq=100)
+    assert s.attempts == len(g["kdv_IF45DP_s"])
+    np.testing.assert_allclose([r[2] for r in s.log], g["kdv_IF45DP_s"], rtol=1e-8)
+    np.testing.assert_allclose(s.t, g["kdv_IF45DP_t"], rtol=1e-12)
+    assert _close(uf, g["kdv_IF45DP_final"], 1e-10)
