@@ -87,8 +87,8 @@ typedef struct rk_controller {
  * r_j psi(r_j) / (r_j - c z) for each scaled argument c z (etd35.py:602-658,
  * etd34.py:366-383, etd4.py:245-262, etd5.py); applied to the eigenvalues of a
  * diagonalizable lin_op this reproduces the reference's psi-matrices
- * S diag(.) S^-1.  0: the diagonal rule (direct formula, contour around z below
- * modecutoff). */
+ * S diag(.) S^-1 (rk_coeffs; rk_evolve refuses it).  0: the diagonal rule (direct formula,
+ * contour around z below modecutoff). */
 typedef struct rk_etd_config {
   double modecutoff;
   double contour_radius;

@@ -208,6 +208,10 @@ int validate_batch(const rk_batch* b, bool need_scratch) {
     set_error("rk_evolve: contour_points must be > 1");
     return RK_E_ARG;
   }
+  if (b->etd.contour_at_zero) {
+    set_error("rk_evolve: contour_at_zero is the matrix-operator form of rk_coeffs, not a diagonal evolve");
+    return RK_E_UNSUPPORTED;
+  }
   if (b->threads != 0 && b->threads != 32 && b->threads != 64 && b->threads != 128 && b->threads != 256) {
     set_error("rk_evolve: threads must be 0 (auto), 32, 64, 128 or 256");
     return RK_E_ARG;

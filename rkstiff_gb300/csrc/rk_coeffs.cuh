@@ -43,7 +43,6 @@ struct EtdCfg {
   double cutoff;
   double R;
   int np;
-  int zero;  // contour_at_zero: every mode by the zero-centred resolvent contour
 };
 
 // The contour node r_j = R exp(2 pi i (j + 1/2)/Np) (rkstiff/etd35.py:259).

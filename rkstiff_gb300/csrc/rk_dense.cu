@@ -855,7 +855,7 @@ extern "C" int rk_dense_evolve(const rk_dense_batch* b, void* stream) {
   p.n = b->n;
   p.err_eigen = b->err_eigen ? 1 : 0;
   p.ctl = b->ctl;
-  p.ec = EtdCfg{b->etd.modecutoff, b->etd.contour_radius, b->etd.contour_points, 0};
+  p.ec = EtdCfg{b->etd.modecutoff, b->etd.contour_radius, b->etd.contour_points};
   CUtensorMap tmA, tmV;
   if (int e = make_map(&tmA, p.A, DM, (int64_t)NMAT * 2 * DM, DM)) return e;
   if (int e = make_map(&tmV, p.V, DM, (int64_t)NVEC * 2 * L.bpad, NT)) return e;

@@ -1008,7 +1008,7 @@ extern "C" int rk_dense_eig_evolve(const rk_dense_eig_batch* b, void* stream) {
   p.first = b->first ? 1 : 0;
   p.max_attempts = b->max_attempts;
   p.ctl = b->ctl;
-  p.ec = EtdCfg{b->etd.modecutoff, b->etd.contour_radius, b->etd.contour_points, 0};
+  p.ec = EtdCfg{b->etd.modecutoff, b->etd.contour_radius, b->etd.contour_points};
   if (p.first) {
     setup_kernel<<<(DM * DM + 255) / 256, 256, 0, s>>>(reinterpret_cast<float*>(w + L.a),
                                                        reinterpret_cast<double*>(w + L.eig),

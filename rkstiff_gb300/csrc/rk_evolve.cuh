@@ -50,6 +50,10 @@ RK_HD int traits_nv(int method) { return traits_nn(method) + (unew_in_n2(method)
 // bytes of an instance's scratch: u, unew, N1..NN (complex T), the coefficient block and,
 // in FP32, a working-precision copy of the wavenumbers (read once per nonlinear evaluation
 // per mode; converting the FP64 input there would put a conversion per mode on the FP64 pipe)
+// bytes after the coefficient blocks: their h tags (RK_COEF_BLOCKS_MAX doubles) and the
+// index of the block the next miss replaces
+constexpr int64_t RK_TAG_BYTES = 8 * (RK_COEF_BLOCKS_MAX + 4);
+
 RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m, int blocks = 1) {
   const int64_t mp = round_up4(m);
   const int64_t ts = precision == RK_FP64 ? 8 : 4;
@@ -57,7 +61,7 @@ RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m,
   const int64_t coef = (coef_complex ? 2 : 1) * ts * mp;
   const int64_t kxw = precision == RK_FP64 ? 0 : ts * mp;
   // with several coefficient blocks: the extra blocks, then their h tags
-  const int64_t extra = blocks > 1 ? (blocks - 1) * num_coeffs(method) * coef + 8 * RK_COEF_BLOCKS_MAX : 0;
+  const int64_t extra = blocks > 1 ? (blocks - 1) * num_coeffs(method) * coef + RK_TAG_BYTES : 0;
   return traits_nv(method) * vec + num_coeffs(method) * coef + kxw + extra;
 }
 
@@ -71,7 +75,7 @@ RK_DEV double ladder_rung(double h0, int k) { return h0 * k_ladder[k & 15] * lde
 
 // the rung h0 * 2^(k/16) (k an integer) nearest to h, or (floor) the largest not above h;
 // the rung is picked in FP32, the floor checked in FP64
-RK_DEV double ladder_step(double h, double h0, bool floor_) {
+static __device__ __noinline__ double ladder_step(double h, double h0, bool floor_) {
   const float l = 16.f * log2f((float)(h / h0));
   int k = floor_ ? (int)floorf(l + 1e-3f) : (int)rintf(l);
   double v = ladder_rung(h0, k);
@@ -135,7 +139,7 @@ __device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off,
   constexpr int n = 1 << LOGN, M = n >> 1;
   // last inverse pass writes the real product u*ux; the forward transform of length n/2
   // reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
-  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [](cx<T>* y, int idx, cx<T> v) {
+  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [](cx<T>* y, int idx, int, cx<T> v) {
     reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
   });
   cx<T>* other = (w == fa) ? fb : fa;
@@ -156,12 +160,12 @@ __device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off,
 template <class T, int LOGN>
 __device__ __noinline__ void nls_core(Group g, cx<T>* fa, cx<T>* fb, const cx<T>* tws, T c,
                                       cx<T>* __restrict__ out) {
-  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [c](cx<T>* y, int idx, cx<T> v) {
+  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [c](cx<T>* y, int, int pidx, cx<T> v) {
     T a2 = (v.x * v.x + v.y * v.y) * c;
-    y[fpad(idx)] = cx<T>{-a2 * v.y, a2 * v.x};
+    y[pidx] = cx<T>{-a2 * v.y, a2 * v.x};
   });
   cx<T>* other = (w == fa) ? fb : fa;
-  fft_ct<T, LOGN, false, LOGN>(g, w, other, tws, [out](cx<T>*, int idx, cx<T> v) { out[idx] = v; });
+  fft_ct<T, LOGN, false, LOGN>(g, w, other, tws, [out](cx<T>*, int idx, int, cx<T> v) { out[idx] = v; });
 }
 
 template <class T, class CT, int LOGN, class KF>
@@ -326,46 +330,6 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
-  if (ec.zero) {
-    // the reference's matrix form on each mode: warp per mode, lanes over the nodes r_q,
-    // summands r_q psi_k(r_q) / (r_q - c z) (psi of the node, the resolvent of the scaled z)
-    const int lane = g.tid & 31, warp = g.tid >> 5, nwarp = g.nthr >> 5;
-    for (int j = warp; j < m; j += nwarp) {
-      S z = load_z<S>(lin, j, h);
-      const cx<double> zc = to_cx(z);
-      cx<double> acc[NP];
-#pragma unroll
-      for (int k = 0; k < NP; ++k) acc[k] = cx<double>{0.0, 0.0};
-      for (int q = lane; q < ec.np; q += 32) {
-        const cx<double> r = contour_node(ec, q);
-        const cx<double> e = cexp(r);
-        const cx<double> p1 = psi1(r, e), p2 = psi2(r, e), p3 = psi3(r, e);
-#pragma unroll
-        for (int k = 0; k < NP; ++k) {
-          int order;
-          double num, den;
-          psi_slot(METHOD, k, order, num, den);
-          const cx<double> cz = (num == 1.0 && den == 1.0) ? zc : rdiv(num * zc, den);
-          const cx<double> pv = order == 1 ? p1 : (order == 2 ? p2 : p3);
-          acc[k] = acc[k] + (r * pv) * crecip(r - cz);
-        }
-      }
-      S P[NP];
-#pragma unroll
-      for (int k = 0; k < NP; ++k) {
-        double re = warp_sum(acc[k].x), im = warp_sum(acc[k].y);
-        P[k] = from_cx<S>(rdiv(h * cx<double>{re, im}, (double)ec.np));
-      }
-      if (lane == 0) {
-        S o[NC];
-        etd_from_psi<S>(METHOD, z, P, o);
-#pragma unroll
-        for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
-      }
-    }
-    g.sync();
-    return;
-  }
   const dd hdd = dd_from_double(h);
   // pass 1: thread per mode, direct formula for |z| >= modecutoff; with FAST the small
   // modes are evaluated here too, by the Taylor series of psi_k (see taylor_psi)
@@ -906,6 +870,77 @@ RK_DEV bool ring_write(const rk_batch& b, int inst, const Group& g, const cx<T>*
 // ---------------------------------------------------------------------------------
 enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 
+// Coefficient blocks of one instance (rk_batch.coef_blocks = nblk > 1), in its global slab:
+// block i at C0 + i * NC * mp, the blocks' h tags and the index of the block the next miss
+// replaces after them.  Kept out of line: the learned controller's ladder uses them, the
+// plain path does not, and their state would otherwise sit in registers through every
+// transform.
+template <class T, class CT, int METHOD>
+RK_DEV unsigned char* slab_of(const rk_batch& b, int inst) {
+  return reinterpret_cast<unsigned char*>(b.slab) + b.slab_off[inst];
+}
+template <class T, class CT, int METHOD>
+RK_DEV CT* coef_block0(const rk_batch& b, int inst, int mp) {
+  constexpr int NV = Traits<METHOD>::NN + (unew_in_n2(METHOD) ? 1 : 2);
+  constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
+  cx<T>* gsl = reinterpret_cast<cx<T>*>(slab_of<T, CT, METHOD>(b, inst));
+  return reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NV * mp) + KXW * mp);
+}
+template <class T, class CT, int METHOD>
+RK_DEV double* coef_tags(const rk_batch& b, int inst, int m, int nblk) {
+  const int64_t bytes = slab_bytes(METHOD, sizeof(T) == 8 ? RK_FP64 : RK_FP32, sizeof(CT) == 2 * sizeof(T), m, nblk);
+  return reinterpret_cast<double*>(slab_of<T, CT, METHOD>(b, inst) + bytes - RK_TAG_BYTES);
+}
+
+// Points C at the block whose tag is h; returns false then.  Otherwise takes the next block in
+// turn, tags it with h (after a barrier: every thread has read the tags before one changes
+// them) and returns true -- the caller rebuilds that block, and compute_coeffs' closing
+// barrier publishes the new tag.
+template <class T, class CT, int METHOD>
+__device__ __noinline__ bool coef_block(const rk_batch& b, int inst, Group g, int mp, int m, int nblk, double h,
+                                        CT*& C) {
+  double* tags = coef_tags<T, CT, METHOD>(b, inst, m, nblk);
+  CT* const C0 = coef_block0<T, CT, METHOD>(b, inst, mp);
+  const int64_t blk = (int64_t)Traits<METHOD>::NC * mp;
+  int hit = -1;
+  for (int i = 0; i < nblk; ++i)
+    if (tags[i] == h) hit = i;
+  if (hit >= 0) {
+    C = C0 + hit * blk;
+    return false;
+  }
+  long long* next = reinterpret_cast<long long*>(tags + RK_COEF_BLOCKS_MAX);
+  const int victim = (int)(*next % nblk);
+  g.sync();
+  if (g.tid == 0) {
+    tags[victim] = h;
+    *next = victim + 1;
+  }
+  C = C0 + victim * blk;
+  return true;
+}
+
+// At the start of a launch: h_coeff NaN (a fresh record, or a noalloc call) invalidates every
+// tag; otherwise C points at the block tagged h_coeff, and if none is, h_coeff is dropped.
+template <class T, class CT, int METHOD>
+__device__ __noinline__ double coef_block_resume(const rk_batch& b, int inst, Group g, int mp, int m, int nblk,
+                                                 double hc, CT*& C) {
+  double* tags = coef_tags<T, CT, METHOD>(b, inst, m, nblk);
+  if (hc != hc) {
+    g.sync();
+    if (g.tid < RK_COEF_BLOCKS_MAX) tags[g.tid] = __longlong_as_double(0x7ff8000000000000ULL);
+    if (g.tid == 0) *reinterpret_cast<long long*>(tags + RK_COEF_BLOCKS_MAX) = 0;
+    g.sync();
+    return hc;
+  }
+  int found = -1;
+  for (int i = 0; i < nblk; ++i)
+    if (tags[i] == hc) found = i;
+  if (found < 0) return __longlong_as_double(0x7ff8000000000000ULL);  // rebuild before the first attempt
+  C = coef_block0<T, CT, METHOD>(b, inst, mp) + found * (int64_t)Traits<METHOD>::NC * mp;
+  return hc;
+}
+
 // u <- unew after an accepted step.  With the new state in N2's array the two arrays swap
 // roles: the old u array becomes N2 (and the next new state's home).
 template <bool U2, class X>
@@ -945,7 +980,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
   x.cf = make_ctlf(b.ctl);
-  const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points, b.etd.contour_at_zero};
+  const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
   const rk_controller ctl = b.ctl;
 
   rk_inst_state st = b.state[inst];
@@ -983,31 +1018,10 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
 
   double t = st.t, tf = st.tf, h = st.h;
   double hc = PLACE == PL_SMEM_ALL ? nan_d() : st.h_coeff;
-  // Coefficient blocks (b.coef_blocks > 1): block i at C0 + i * blk, its h tag in the slab
-  // after the blocks (tags[i], persistent across launches).  A stale record (h_coeff NaN:
-  // fresh state, or a noalloc call) invalidates every tag.
+  // Coefficient blocks (b.coef_blocks > 1): see coef_block / coef_block_resume
   const int nblk =
       (!Tr::ADAPT || PLACE == PL_SMEM_ALL || b.coef_blocks <= 1) ? 1 : min(b.coef_blocks, RK_COEF_BLOCKS_MAX);
-  CT* const C0 = x.C;
-  const int64_t blk = (int64_t)Tr::NC * x.mp;
-  double* tags = nblk > 1 ? reinterpret_cast<double*>(
-                                reinterpret_cast<unsigned char*>(gsl) +
-                                (slab_bytes(METHOD, sizeof(T) == 8 ? RK_FP64 : RK_FP32, sizeof(CT) == 2 * sizeof(T), x.m,
-                                            nblk) - 8 * RK_COEF_BLOCKS_MAX))
-                          : nullptr;
-  int victim = 0;
-  if (nblk > 1) {
-    if (hc != hc) {
-      if (g.tid < RK_COEF_BLOCKS_MAX) tags[g.tid] = nan_d();
-      g.sync();
-    } else {
-      int found = -1;
-      for (int i = 0; i < nblk; ++i)
-        if (tags[i] == hc) found = i;
-      if (found >= 0) x.C = C0 + found * blk;
-      else hc = nan_d();  // no block holds h_coeff: rebuild before the first attempt
-    }
-  }
+  if (nblk > 1) hc = coef_block_resume<T, CT, METHOD>(b, inst, g, x.mp, x.m, nblk, hc, x.C);
   // the learned controller's step-size ladder starts at the instance's first step size
   const bool ladder = Tr::ADAPT && b.ladder != 0 && b.mlp != nullptr;
   double h0 = st.reserved_d;
@@ -1034,17 +1048,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       double hs = h;
       for (;;) {
         if (h != hc) {  // exact compare, as the reference's _update_coeffs
-          int hit = -1;
-          for (int i = 0; i < nblk && nblk > 1; ++i)
-            if (tags[i] == h) hit = i;
-          if (hit >= 0) {
-            x.C = C0 + hit * blk;
-          } else {
-            if (nblk > 1) {
-              x.C = C0 + victim * blk;
-              if (g.tid == 0) tags[victim] = h;  // published by compute_coeffs' closing barrier
-              victim = (victim + 1) % nblk;
-            }
+          if (nblk <= 1 || coef_block<T, CT, METHOD>(b, inst, g, x.mp, x.m, nblk, h, x.C)) {
             compute_coeffs<T, CT, S, METHOD>(x, h, ec);
             ++coeff_updates;
           }
@@ -1250,11 +1254,59 @@ __global__ void coeff_kernel(int m, const double* lin, double h, rk_etd_config e
   const Group g{(int)threadIdx.x, (int)blockDim.x, 0};
   const int per = blockDim.x;
   const int j0 = blockIdx.x * per;
-  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points, etd.contour_at_zero};
+  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points};
   // arrays of length m, shifted so that c*m + j addresses mode j0 + j
   compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(g, min(per, m - j0), m,
                                                                 reinterpret_cast<const cx<double>*>(lin) + j0,
                                                                 out + j0, h, ec);
+}
+
+// Coefficients with the reference's matrix-form psi values (rk_etd_config.contour_at_zero):
+// for each mode the mean over the zero-centred contour nodes r_q of r_q psi_k(r_q) /
+// (r_q - c z), c the scale of the slot -- the reference's non-diagonal psi-matrices
+// (etd35.py:602-658) on one eigenvalue.  A warp per mode, lanes over the nodes; its own
+// kernel, so that none of its registers weigh on the stepping kernels.
+template <class CT, class S, int METHOD>
+__global__ void coeff_zero_contour_kernel(int m, const double* lin_, double h, rk_etd_config etd, CT* C) {
+  constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
+  constexpr int NC = Traits<METHOD>::NC;
+  const cx<double>* lin = reinterpret_cast<const cx<double>*>(lin_);
+  const EtdCfg ec{etd.modecutoff, etd.contour_radius, etd.contour_points};
+  const int mp = m;
+  const int lane = threadIdx.x & 31;
+  const int j = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  if (j >= m) return;
+  S z = load_z<S>(lin, j, h);
+  const cx<double> zc = to_cx(z);
+  cx<double> acc[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) acc[k] = cx<double>{0.0, 0.0};
+  for (int q = lane; q < ec.np; q += 32) {
+    const cx<double> r = contour_node(ec, q);
+    const cx<double> e = cexp(r);
+    const cx<double> p1 = psi1(r, e), p2 = psi2(r, e), p3 = psi3(r, e);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      int order;
+      double num, den;
+      psi_slot(METHOD, k, order, num, den);
+      const cx<double> cz = (num == 1.0 && den == 1.0) ? zc : rdiv(num * zc, den);
+      const cx<double> pv = order == 1 ? p1 : (order == 2 ? p2 : p3);
+      acc[k] = acc[k] + (r * pv) * crecip(r - cz);
+    }
+  }
+  S P[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    double re = warp_sum(acc[k].x), im = warp_sum(acc[k].y);
+    P[k] = from_cx<S>(rdiv(h * cx<double>{re, im}, (double)ec.np));
+  }
+  if (lane == 0) {
+    S o[NC];
+    etd_from_psi<S>(METHOD, z, P, o);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+  }
 }
 
 // bytes of the per-instance arrays held in shared memory under placement `place`

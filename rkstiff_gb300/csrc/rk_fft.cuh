@@ -216,16 +216,21 @@ struct PassRadix {
 };
 
 // One Stockham pass of radix R = 2^LGR at sub-length Ls = 2^LGLS over N = 2^LOGN points.
-// `post(idx, value)` receives the output (final pass) -- by default a store to y.
+// `store(idx, pidx, value)` receives each output with its unpadded index and its padded
+// position fpad(idx).  With power-of-two R, Ls and NB the padded positions of a butterfly's
+// inputs i + r NB and outputs j + r Ls are its base position plus compile-time offsets
+// (fpad(a + b) = fpad(a) + b + (b >> 4) for these b), so each load and store needs no
+// index arithmetic of its own.
 template <class T, int LOGN, int LGR, int LGLS, bool INV, int TWLOG, class Store>
 RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ tw, Store store) {
   constexpr int N = 1 << LOGN, R = 1 << LGR, Ls = 1 << LGLS, NB = N / R;
   constexpr int TWS = (1 << TWLOG) >> (LGLS + LGR);  // table stride of W_{R Ls}
   for (int i = g.tid; i < NB; i += g.nthr) {
     const int k = i & (Ls - 1);
+    const cx<T>* xi = x + fpad(i);
     cx<T> v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = x[fpad(i + r * NB)];
+    for (int r = 0; r < R; ++r) v[r] = xi[r * NB + ((r * NB) >> 4)];
     if constexpr (Ls > 1) {
       // twiddle tables of 2^TWLOG <= 4096 entries live in shared memory at padded
       // positions (strided reads would otherwise fall into a few banks)
@@ -234,8 +239,9 @@ RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<
     }
     dft_reg<T, R, INV>(v);
     const int j = ((i - k) << LGR) + k;
+    const int pj = fpad(j);
 #pragma unroll
-    for (int r = 0; r < R; ++r) store(j + r * Ls, v[r]);
+    for (int r = 0; r < R; ++r) store(j + r * Ls, pj + r * Ls + ((r * Ls) >> 4), v[r]);
   }
 }
 
@@ -245,11 +251,11 @@ RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw,
   constexpr int DONE = PassRadix<LOGN, P>::bits_before();
   if constexpr (DONE + LGR == LOGN) {
     // final pass: outputs go to fin(y, index, value); y is the buffer not being read
-    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, cx<T> v) { fin(y, idx, v); });
+    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, int pidx, cx<T> v) { fin(y, idx, pidx, v); });
     g.sync();
     return y;
   } else {
-    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, cx<T> v) { y[fpad(idx)] = v; });
+    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int, int pidx, cx<T> v) { y[pidx] = v; });
     g.sync();
     return fft_ct_passes<T, LOGN, P + 1, INV, TWLOG>(g, y, x, tw, fin);
   }
@@ -258,8 +264,8 @@ RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw,
 // FFT of 2^LOGN points held in `a` at padded positions fpad(i) (`b` is scratch of the same
 // size), with `tw` a table of the 2^TWLOG twiddles exp(-2 pi i k/2^TWLOG), TWLOG >= LOGN,
 // stored at padded positions fpad(k).
-// The final pass hands every output to fin(y, index, value), where y is the buffer that
-// pass does not read and `index` the unpadded output index; returns y.  All group threads
+// The final pass hands every output to fin(y, index, padded index, value), where y is the
+// buffer that pass does not read and `index` the unpadded output index; returns y.  All group threads
 // call.
 template <class T, int LOGN, bool INV, int TWLOG, class FinalStore>
 RK_DEV cx<T>* fft_ct(const Group& g, cx<T>* a, cx<T>* b, const cx<T>* tw, FinalStore fin) {
@@ -268,7 +274,7 @@ RK_DEV cx<T>* fft_ct(const Group& g, cx<T>* a, cx<T>* b, const cx<T>* tw, FinalS
 
 template <class T>
 struct StoreY {
-  RK_DEV void operator()(cx<T>* y, int idx, cx<T> v) const { y[fpad(idx)] = v; }
+  RK_DEV void operator()(cx<T>* y, int, int pidx, cx<T> v) const { y[pidx] = v; }
 };
 
 }  // namespace rk

@@ -85,6 +85,11 @@ static int launch_evolve_m(const rk_batch& b, const ClassLaunch& c, cudaStream_t
 template <class T, class CT, class S, int M>
 static int launch_coeffs_t(int64_t m, const double* lin, double h, const rk_etd_config& etd, void* out,
                            cudaStream_t st) {
+  if (etd.contour_at_zero && is_etd(M)) {
+    const unsigned blocks = (unsigned)((m * 32 + 255) / 256);  // a warp per mode
+    coeff_zero_contour_kernel<CT, S, M><<<blocks, 256, 0, st>>>((int)m, lin, h, etd, reinterpret_cast<CT*>(out));
+    return cuda_check(cudaGetLastError(), "coefficient launch");
+  }
   const int threads = 256;
   const unsigned blocks = (unsigned)((m + threads - 1) / threads);
   coeff_kernel<T, CT, S, M><<<blocks, threads, 0, st>>>((int)m, lin, h, etd, reinterpret_cast<CT*>(out));

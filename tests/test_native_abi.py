@@ -176,3 +176,13 @@ def test_noalloc_size_check_cannot_overflow(lib):
     b = _fake_batch(2, 3000)
     assert lib.rk_evolve_noalloc(ctypes.byref(b), None) == nat.RK_E_SIZE
     assert b"power of two" in lib.rk_last_error()
+
+
+def test_evolve_refuses_the_matrix_contour_flag(lib):
+    """contour_at_zero is the matrix-operator form of rk_coeffs; rk_evolve refuses it before
+    touching any pointer (so placeholders suffice, and no GPU is needed)."""
+    b = _fake_batch(2, 256)
+    b.slab = b.slab_off = b.queue = 0x1000
+    b.etd = nat.RkEtdConfig(modecutoff=0.01, contour_radius=1.0, contour_points=32, contour_at_zero=1)
+    assert lib.rk_evolve(ctypes.byref(b), None) == nat.RK_E_UNSUPPORTED
+    assert b"contour_at_zero" in lib.rk_last_error()
