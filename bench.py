@@ -195,6 +195,23 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
+TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "ks_ensemble_etd35_fp32_traffic.md")
+
+
+def profiled_traffic():
+    """DRAM bytes (read + write) of one headline launch, summed over its grid-size class
+    kernels, from the committed summary of an ncu capture of that launch (a line
+    'traffic_bytes_per_launch: N'); None when the summary is absent."""
+    try:
+        with open(TRAFFIC_SUMMARY) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
 def flops_of(ens_engine, st) -> float:
     """Algorithmic FP32 FLOPs of one launch from its counters: per nonlinear evaluation
     7.5 n log2 n + n + 2m (one complex inverse FFT of n, one forward of n/2, the product
@@ -701,7 +718,10 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
             "peak": peak,
             "unit": "TFLOP/s",
             "frac": achieved / peak,
-            "traffic": None,
+            "traffic": profiled_traffic(),
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one headline launch (all class "
+                              "kernels), ncu capture summarised in profiles/ks_ensemble_etd35_fp32_traffic.md",
+            "algorithmic_bytes": 2 * vec_bytes + state_bytes,
             "peak_source": "measured in this run by rk_probe_fp32 (FP32 FMA throughput; "
                            "MEASURED_PEAKS.json carries no FP32 CUDA-core figure)",
             "flops_per_launch": flops / max(n_launch, 1),
