@@ -20,6 +20,7 @@ import argparse
 import json
 import multiprocessing as mp
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -198,18 +199,52 @@ class ClockSampler:
 TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "ks_ensemble_etd35_fp32_traffic.md")
 
 
-def profiled_traffic():
-    """DRAM bytes (read + write) of one headline launch, summed over its grid-size class
-    kernels, from the committed summary of an ncu capture of that launch (a line
-    'traffic_bytes_per_launch: N'); None when the summary is absent."""
+PLACE_NAMES = {0: "global", 1: "smem-state", 2: "smem-all"}
+
+
+def shape_tag(n, threads, groups, place) -> str:
+    return "n=%d %dx%d/%s" % (n, threads, groups, PLACE_NAMES[place])
+
+
+def profiled_traffic(tuned):
+    """DRAM bytes (read + write) of one headline launch: the sum over its grid-size class
+    kernels of the per-class figures in the committed summary of ncu captures of that launch
+    (lines 'traffic n=<n> <threads>x<groups>/<placement>: <bytes>').  A class kernel's traffic
+    depends on its launch shape (global scratch writes its stage vectors back), so each class
+    is looked up under the shape this run used; returns (bytes or None, [missing shapes])."""
+    table = {}
     try:
         with open(TRAFFIC_SUMMARY) as f:
             for line in f:
-                if line.strip().startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":", 1)[1].strip().split()[0])
+                m = re.match(r"\s*traffic (n=\d+ \d+x\d+/[a-z-]+):\s*(\d+)", line)
+                if m:
+                    table[m.group(1)] = float(m.group(2))
     except OSError:
         pass
-    return None
+    total, missing = 0.0, []
+    for n, v in tuned.items():
+        tag = shape_tag(int(n), v["threads"], v["groups"], v["place"])
+        if tag in table:
+            total += table[tag]
+        else:
+            missing.append(tag)
+    return (None if missing else total), missing
+
+
+def pin_shapes(ens, spec: str):
+    """Install launch shapes given as 'n:TxG:placement,...' (e.g. '2048:128x1:global') for
+    every grid-size class, in place of the tuner's choice."""
+    from rkstiff_gb300 import autotune as _at
+    by_n = {}
+    for item in spec.split(","):
+        n, tg, place = item.split(":")
+        t, g = tg.split("x")
+        by_n[int(n)] = (int(t), int(g), {v: k for k, v in PLACE_NAMES.items()}[place])
+    eng = ens.engine
+    missing = [int(n) for n in eng.class_n if int(n) not in by_n]
+    if missing:
+        raise SystemExit(f"--shapes gives no shape for grid size(s) {missing}")
+    _at._CACHE[_at._key(eng)] = tuple(by_n[int(n)] for n in eng.class_n)
 
 
 def flops_of(ens_engine, st) -> float:
@@ -595,7 +630,10 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
                    device=dev)
     eng = ens.engine
     from rkstiff_gb300 import autotune as _at
-    if args.tune_cache and _at.load(args.tune_cache):
+    if args.shapes:
+        pin_shapes(ens, args.shapes)
+        tuned = ens.autotune(u0s, span=10.0)  # served from the pinned shapes
+    elif args.tune_cache and _at.load(args.tune_cache):
         tuned = ens.autotune(u0s, span=10.0)  # served from the loaded cache
     else:
         tuned = ens.autotune(u0s, span=10.0)
@@ -610,6 +648,7 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
         # class kernel of the persistent evolve launch
         return ens.evolve_graph(u, u0_dev, 0.0, tf)
 
+    l2_flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     for _ in range(args.warmup):
         st = one_step()
     torch.cuda.synchronize()
@@ -629,24 +668,25 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    marks = [e0]
-    for _ in range(args.steps):
+    pairs = []
+    for i in range(args.steps):
+        # L2 flush between timed steps: a write larger than the 129 MB L2, outside the
+        # step's own event pair
+        l2_flush.fill_(i & 0xFF)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
         st = one_step()
+        b.record(stream)
+        pairs.append((a, b))
         mode_steps += int(np.sum(eng.ms * st["steps"]))
         flops += flops_of(eng, st)
-        mark = torch.cuda.Event(enable_timing=True)
-        mark.record(stream)
-        marks.append(mark)
-    e1.record(stream)
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
     eng.record_events = False
-    elapsed = e0.elapsed_time(e1) * 1e-3
+    elapsed = sum(a.elapsed_time(b) for a, b in pairs) * 1e-3
     kernel_s = sum(a.elapsed_time(b) for a, b in eng.events) * 1e-3
     n_launch = eng.launches - launches0
     n_kernels = eng.kernel_launches - kernels0
@@ -659,16 +699,19 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
     host_in = torch.empty(u0_dev.shape, dtype=u0_dev.dtype, pin_memory=True)
     host_in.copy_(u0_dev.cpu())
     host_out = torch.empty_like(host_in, pin_memory=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
     e2e_mode_steps = 0
-    for _ in range(args.steps):
+    e2e_s = 0.0
+    for i in range(args.steps):
+        l2_flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         u0_dev.copy_(host_in, non_blocking=True)
         st2 = ens.evolve_graph(u, u0_dev, 0.0, tf)
         host_out.copy_(u, non_blocking=True)
         torch.cuda.synchronize()
+        e2e_s += time.perf_counter() - t0
         e2e_mode_steps += int(np.sum(eng.ms * st2["steps"]))
-    e2e_elapsed = sharding.max_over_ranks(time.perf_counter() - t0, dev)
+    e2e_elapsed = sharding.max_over_ranks(e2e_s, dev)
     e2e_value = sharding.sum_over_ranks(e2e_mode_steps, dev) / e2e_elapsed
     state_bytes = eng.state_dev.numel()
     vec_bytes = u.numel() * u.element_size()
@@ -685,6 +728,7 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
     if dense is not None:
         dense["cpu_baseline"] = dense_cpu
     achieved = flops / kernel_s / 1e12
+    traffic, traffic_missing = profiled_traffic(tuned)
     counts = {name: int(np.sum(status == code)) for name, code in (("done", 0), ("max_loops", 1), ("min_step", 2))}
     line = {
         "metric": METRIC,
@@ -694,7 +738,7 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": max_elapsed / args.steps * 1e3,
-        "step_ms": [round(a.elapsed_time(b), 3) for a, b in zip(marks[:-1], marks[1:])],
+        "step_ms": [round(a.elapsed_time(b), 3) for a, b in pairs],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -704,13 +748,13 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
             **{k: WORKLOAD[k] for k in ("workload", "instances", "n_choices", "L_range", "epsilon", "tf", "method")},
             "precision": "fp32",
             "launch": "one persistent launch per step, replayed from a captured CUDA graph",
+            "schedule": "per grid-size class, longest first by the previous launch's attempt counts "
+                        "(set after the first warm-up step; the order does not change any instance's result)",
             "parallelism": f"instances per GPU, {world} GPU(s)",
-            "l2_flush": "not needed: per-step working set (%d MB scratch + states) exceeds the 126 MB L2"
-                        % (eng.slab_bytes // (1 << 20)),
+            "l2_flush": "256 MB written between timed steps, outside each step's event pair",
             "instance_status": counts,
             "launch_shapes": {str(n): "%d groups x %d threads per block, %s scratch" % (
-                v["groups"], v["threads"], {0: "global", 1: "smem-state", 2: "smem-all"}[v["place"]])
-                for n, v in tuned.items()},
+                v["groups"], v["threads"], PLACE_NAMES[v["place"]]) for n, v in tuned.items()},
         },
         "roofline": {
             "bound": "fp32",
@@ -718,9 +762,12 @@ def gpu_arm(args, rank, world, cpu_line, dense_cpu=None, extra=None):
             "peak": peak,
             "unit": "TFLOP/s",
             "frac": achieved / peak,
-            "traffic": profiled_traffic(),
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one headline launch (all class "
-                              "kernels), ncu capture summarised in profiles/ks_ensemble_etd35_fp32_traffic.md",
+            "traffic": traffic,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per class kernel of one headline "
+                              "launch at this run's launch shapes, summed over the classes; ncu captures "
+                              "summarised in profiles/ks_ensemble_etd35_fp32_traffic.md"
+                              + ("" if traffic is not None else
+                                 "; no capture for " + ", ".join(traffic_missing)),
             "algorithmic_bytes": 2 * vec_bytes + state_bytes,
             "peak_source": "measured in this run by rk_probe_fp32 (FP32 FMA throughput; "
                            "MEASURED_PEAKS.json carries no FP32 CUDA-core figure)",
@@ -900,6 +947,9 @@ def main():
     ap.add_argument("--no-dense", action="store_true", help="skip the dense Allen-Cahn measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-instance configs (KS n=1024, NLS n=4096)")
     ap.add_argument("--tune-cache", default="", help="JSON file of tuned launch shapes to load, or to write")
+    ap.add_argument("--shapes", default="",
+                    help="pin the launch shape of every grid-size class, e.g. "
+                         "'2048:128x1:global,1024:128x1:global,512:128x1:smem-all,256:64x2:smem-all'")
     ap.add_argument("--instances", type=int, default=WORKLOAD["instances"], help="smaller cases for profiling")
     ap.add_argument("--sizes", default="", help="comma-separated subset of the grid sizes (profiling)")
     ap.add_argument("--tf", type=float, default=WORKLOAD["tf"], help="final time (profiling)")

@@ -6,7 +6,8 @@ One ``DiagEnsemble`` holds, on one CUDA device:
 * the operators (complex128, concatenated by mode offset) and wavenumbers (float64),
 * the per-instance scratch ("slab": the coefficient block, u/unew and the stage arrays),
 * the per-instance controller state records (``STATE_DTYPE``),
-* the processing order (largest grid first, so the tail of a persistent launch is short).
+* the processing order (largest grid first; within a grid size, longest first by the
+  previous evolve's attempt counts, so the tail of a persistent launch is short).
 
 The solver classes use a one-instance ensemble; ``rkstiff_gb300.ensemble`` exposes the
 batched form directly.
@@ -144,7 +145,11 @@ class DiagEnsemble:
         self.off_dev = torch.from_numpy(self.mode_off).to(dev)
         # largest grids first; instances of equal n form one class (one kernel each)
         order = np.argsort(-self.ns, kind="stable").astype(np.int32)
+        self._size_order = order
         self.order_dev = torch.from_numpy(order).to(dev)
+        # "history": after each evolve the queue of every class is reordered longest-first
+        # by that evolve's attempt counts (reorder_by_cost); "size": index order within a class
+        self.schedule = "history"
         sorted_n = self.ns[order]
         bounds = [0] + [i for i in range(1, n_inst) if sorted_n[i] != sorted_n[i - 1]] + [n_inst]
         self.class_n = np.ascontiguousarray([int(sorted_n[b]) for b in bounds[:-1]], dtype=np.int32)
@@ -218,6 +223,25 @@ class DiagEnsemble:
         st["s_last"] = np.nan
         st["status"] = nat.RK_ST_RUNNING
         return st
+
+    def reorder_by_cost(self, cost) -> None:
+        """Reorder the work queue of every grid-size class longest-first by ``cost`` (one
+        value per instance, e.g. the attempts of the previous evolve): a persistent launch
+        then starts the longest instances first and ends on short ones, which shortens the
+        tail where a class's last instances run while its other blocks have exited.  Each
+        instance's arithmetic does not depend on the order, so results are unchanged."""
+        cost = np.asarray(cost)
+        if cost.shape != (self.n_inst,):
+            raise ValueError("one cost per instance is required")
+        order = self._size_order.copy()
+        for c in range(len(self.class_n)):
+            a, b = int(self.class_start[c]), int(self.class_start[c + 1])
+            idx = order[a:b]
+            order[a:b] = idx[np.argsort(-cost[idx], kind="stable")]
+        self.order_dev.copy_(torch.from_numpy(order))
+
+    def reset_order(self) -> None:
+        self.order_dev.copy_(torch.from_numpy(self._size_order))
 
     def put_state(self, st: np.ndarray) -> None:
         self.state_dev.copy_(torch.from_numpy(np.ascontiguousarray(st).view(np.uint8)))

@@ -33,10 +33,14 @@ class Ensemble:
     nl_funcs : per-instance :class:`BuiltinNL` (same kind and constant for all)
     config, etd_config : SolverConfig / ETDConfig shared by all instances
     precision : 'fp32' (default) or 'fp64'
+    schedule : 'history' (default: after each evolve, every grid-size class is queued
+        longest-first by that evolve's attempt counts) or 'size' (index order)
     """
 
     def __init__(self, method: str, lin_ops: Sequence, nl_funcs: Sequence[BuiltinNL], config=None, etd_config=None,
-                 precision: str = "fp32", device=None, threads: int = 0):
+                 precision: str = "fp32", device=None, threads: int = 0, schedule: str = "history"):
+        if schedule not in ("history", "size"):
+            raise ValueError("schedule must be 'history' or 'size'")
         if len(nl_funcs) != len(lin_ops):
             raise ValueError("one nonlinearity per instance is required")
         kinds = {(nl.kind, nl.coef) for nl in nl_funcs}
@@ -51,6 +55,7 @@ class Ensemble:
         self.engine = DiagEnsemble(method, lin_ops, nl0.kind, nl0.coef, kxs, [nl.n for nl in nl_funcs],
                                    precision=precision, config=config, etd_config=etd_config, device=device,
                                    threads=threads)
+        self.engine.schedule = schedule
         self.state = None
         self._lin_ops = list(lin_ops)
         self._kxs = kxs
@@ -93,7 +98,12 @@ class Ensemble:
         except EvolveBoundError as ex:
             self.state = ex.state
             raise
+        self._schedule_from(self.state)
         return self.state
+
+    def _schedule_from(self, st: np.ndarray) -> None:
+        if self.engine.schedule == "history":
+            self.engine.reorder_by_cost(st["attempts"])
 
     def evolve_graph(self, u_dev: torch.Tensor, u0_dev: torch.Tensor, t0: float, tf: float,
                      h_init: Optional[float] = None, max_steps: int = 200_000, max_launches: int = 50) -> np.ndarray:
@@ -123,6 +133,7 @@ class Ensemble:
                 self.state = st
                 raise EvolveBoundError(f"evolve did not reach tf within {max_launches} launches", st)
         self.state = st
+        self._schedule_from(st)
         return st
 
     def evolve(self, u0s: Sequence, t0: float, tf: float, h_init: Optional[float] = None, **bounds):

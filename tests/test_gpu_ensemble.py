@@ -130,3 +130,30 @@ def test_graph_replay_matches_launch():
     ens.evolve_packed(u, 0.0, 5.0)
     ens.evolve_graph(u2, u0, 0.0, 5.0)
     assert torch.equal(u2, u)
+
+
+def test_longest_first_schedule_keeps_results():
+    """The 'history' schedule queues each grid-size class longest-first by the previous
+    evolve's attempts; the states and counters are bit-identical to index order."""
+    inst = ks_instances(per_size=6, seed=21)
+    ens, u0s = build(inst, "fp32")
+    eng = ens.engine
+    u0 = ens.pack(u0s)
+    eng.schedule = "size"
+    u_ref = u0.clone()
+    st_ref = ens.evolve_packed(u_ref, 0.0, 3.0)
+    assert np.array_equal(eng.order_dev.cpu().numpy(), eng._size_order)
+    eng.schedule = "history"
+    u1 = u0.clone()
+    ens.evolve_packed(u1, 0.0, 3.0)  # index order; sets the longest-first order after it
+    order = eng.order_dev.cpu().numpy()
+    assert not np.array_equal(order, eng._size_order)
+    for c in range(len(eng.class_n)):
+        idx = order[eng.class_start[c]:eng.class_start[c + 1]]
+        assert np.all(eng.ns[idx] == eng.class_n[c])
+        assert np.all(np.diff(st_ref["attempts"][idx]) <= 0)
+    u2 = u0.clone()
+    st2 = ens.evolve_packed(u2, 0.0, 3.0)
+    assert torch.equal(u2, u_ref)
+    for k in ("steps", "attempts", "rejects", "nl_evals", "status", "t"):
+        np.testing.assert_array_equal(st2[k], st_ref[k])
