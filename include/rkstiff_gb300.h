@@ -229,7 +229,8 @@ int rk_ring_destroy(rk_ring* r);
 /* learned controller: MLP with RK_MLP_IN inputs, two tanh layers of RK_MLP_H units and one
  * linear output.  Training parameters (FP32, flat): W1[H][IN], b1[H], W2[H][H], b2[H],
  * w3[H], b3 -- RK_MLP_NPARAM floats.  Inference buffer (rk_mlp_pack): float mu[IN],
- * inv_sd[IN], b1[H], b2[H], b3, pad[3], then bf16 W1[H][IN], W2[H][H], w3[H]. */
+ * inv_sd[IN], b1[H], b2[H], b3, pad[3], then bf16 W1[H][IN], W2 transposed ([k][j] holds
+ * W2[j][k], so that consecutive units read consecutive weights), w3[H]. */
 #define RK_MLP_IN 8
 #define RK_MLP_H 64
 #define RK_MLP_NPARAM (RK_MLP_H * RK_MLP_IN + RK_MLP_H + RK_MLP_H * RK_MLP_H + RK_MLP_H + RK_MLP_H + 1)

@@ -177,6 +177,31 @@ RK_DEV void group_sum2_dff(const Group& g, double* red, df a, df b, df& sa, df& 
   sb = tb;
 }
 
+// Group-wide double-float sums of four values (all threads receive them).
+RK_DEV void group_sum4_dff(const Group& g, double* red, df* v) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = warp_sum_df(v[q]);
+  const int nw = g.nthr >> 5;
+  if (nw == 1) return;
+  float* rf = reinterpret_cast<float*>(red);  // 8 floats per warp, <= 16 warps
+  const int w = g.tid >> 5;
+  g.sync();
+  if ((g.tid & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      rf[8 * w + 2 * q] = v[q].hi;
+      rf[8 * w + 2 * q + 1] = v[q].lo;
+    }
+  }
+  g.sync();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    df t{0.f, 0.f};
+    for (int i = 0; i < nw; ++i) t = df_add(t, df{rf[8 * i + 2 * q], rf[8 * i + 2 * q + 1]});
+    v[q] = t;
+  }
+}
+
 // group-wide max of a non-negative FP32 value; NaN anywhere gives NaN
 RK_DEV float group_max_nan_f(const Group& g, double* red, float v, bool nan) {
   v = warp_max_f(nan ? 0.f : v);

@@ -109,9 +109,9 @@ RK_DEV float nl_ac(float w, float x) {
   return x - v * v * v;
 }
 
-// FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): FP32 below
-// z = -STIFF_Z, double-float arithmetic up to z = 80 (the psi Taylor series below
-// modecutoff), FP64 beyond.
+// FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): the stiff
+// form below z = -STIFF_Z, the combinations' FP32 Taylor tables / stiff forms up to z = 80
+// (series_coeffs_f32; IF34's exponentials in double-float), FP64 beyond.
 template <int METHOD>
 RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
   if (z < -(double)STIFF_Z) {
@@ -132,7 +132,7 @@ RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
     constexpr int NP = METHOD == RK_ETD35 ? RK_PSI35_N : RK_PSI34_N;
     constexpr int NC = METHOD == RK_ETD35 ? C35_N : C34_N;
     if (z <= 80.0) {
-      dd_etd_coeffs(METHOD, z, dd_from_double(h), out, fabs(z) < ec.cutoff);
+      series_coeffs_f32<METHOD>(z, h, out);
     } else {
       double E[4], P[NP], o[NC];
       fast_real_psi(METHOD, z, h, E, P);

@@ -114,6 +114,8 @@ struct Ctx {
   const cx<T>* tw;   // global table of RK_TW_N twiddles
   const cx<T>* tws;  // compile-time path: shared-memory table of 2^LOGN twiddles
   CtlF cf;           // FP32 controller constants (FP32 working precision)
+  bool want_tail;    // the attempt's pass over unew also forms the tail-energy fraction
+  mutable float tail_frac;  // that fraction (-1: not formed by the attempt)
   RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
 };
 
@@ -330,7 +332,6 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     return;
   }
   constexpr int NP = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? RK_PSI35_N : RK_PSI34_N;
-  const dd hdd = dd_from_double(h);
   // pass 1: thread per mode, direct formula for |z| >= modecutoff; with FAST the small
   // modes are evaluated here too, by the Taylor series of psi_k (see taylor_psi)
   for (int j = g.tid; j < m; j += g.nthr) {
@@ -342,10 +343,10 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     if constexpr (FAST) {
       if (small) {
         if constexpr (sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float)) {
-          // the series in double-float on the FP32 pipes: the FP64 series would hold the
-          // whole warp on the 1/64-rate FP64 pipe for one small mode
+          // each combination's own Taylor series in FP32 (series_coeffs_f32): the FP64
+          // series would hold the whole warp on the 1/64-rate FP64 pipe for one small mode
           float of[NC];
-          dd_etd_coeffs(METHOD, sre(z), hdd, of, true);
+          series_coeffs_f32<METHOD>(sre(z), h, of);
 #pragma unroll
           for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         } else {
@@ -369,9 +370,9 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
         continue;
       }
       if (zr <= 80.0) {
-        // double-float on the FP32 pipes; the result rounds to the FP64 evaluation's
+        // FP32 series / stiff forms per combination (series_coeffs_f32)
         float of[NC];
-        dd_etd_coeffs(METHOD, zr, hdd, of);
+        series_coeffs_f32<METHOD>(zr, h, of);
 #pragma unroll
         for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         continue;
@@ -591,6 +592,26 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const CtlF
   // NaN keeps every comparison false, as in the reference
   const float thr = cf.cut2 * maxu;
   df au{0.f, 0.f}, ae{0.f, 0.f};
+  if (x.want_tail) {
+    // with the tail-energy fraction of unew (tail_fraction's sums) in the same pass
+    const bool full = x.m == x.n;
+    const int j0 = full ? (3 * x.n) / 8 : (3 * x.m) / 4;
+    const int j1 = full ? (5 * x.n) / 8 : x.m - 1;
+    df v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+      const float a2 = park[2 * j];
+      if (a2 > thr) {
+        v[0] = df_add(v[0], a2);
+        v[1] = df_add(v[1], park[2 * j + 1]);
+      }
+      v[3] = df_add(v[3], a2);
+      if (j >= j0 && j <= j1) v[2] = df_add(v[2], a2);
+    }
+    group_sum4_dff(x.g, x.red, v);
+    const double st = (double)v[2].hi + (double)v[2].lo, sa = (double)v[3].hi + (double)v[3].lo;
+    x.tail_frac = sa > 0.0 ? (float)(st / sa) : 0.f;
+    return s_from_sums_f32_fast(v[0], v[1], cf.log2_eps2, cf.safety, q);
+  }
   for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
     const float a2 = park[2 * j];
     if (a2 > thr) {
@@ -805,6 +826,12 @@ RK_DEV float tail_fraction(const Ctx<T, CT, LOGN>& x) {
 
 RK_DEV float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 RK_DEV float safe_log(double v) { return (v > 0.0 && v < 1e300) ? (float)log(v) : (v > 0.0 ? 690.f : -690.f); }
+// log v clamped to [-8, 8] in FP32 (a NaN or non-positive v gives -8): the learned
+// controller's log s feature, which needs no FP64 log
+RK_DEV float log_clamped8(double v) {
+  const float f = (float)v;
+  return v > 0.0 ? clampf(__logf(f), -8.f, 8.f) : -8.f;
+}
 
 // ---------------------------------------------------------------------------------
 // snapshot stream: one slot of the mapped host ring per snapshot
@@ -980,6 +1007,8 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
   x.cf = make_ctlf(b.ctl);
+  x.want_tail = false;
+  x.tail_frac = -1.f;
   const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
   const rk_controller ctl = b.ctl;
 
@@ -1038,6 +1067,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   // learned-controller features and the attempt log
   const bool learned = Tr::ADAPT && b.mlp != nullptr;
   const bool want_tail = learned || b.attempt_log != nullptr;
+  x.want_tail = want_tail;
   float s_prev = 0.f, s_prev2 = 0.f, acc_prev = 1.f, tail_prev = -1.f;  // log s history starts neutral
   double h_prev = 0.0;
 
@@ -1062,11 +1092,12 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
           if (!(resumed && !n1_valid && Tr::FSAL)) ++nlc;
           n1_valid = true;
         }
+        x.tail_frac = -1.f;
         double s = run_attempt<T, CT, METHOD>(x, h, ctl, nlc);
         nl_evals += nlc;
         s_last = s;
         const bool ok = !(isinf(s) || isnan(s) || s < 1.0);
-        const float tail = want_tail ? tail_fraction(x) : 0.f;
+        const float tail = !want_tail ? 0.f : (x.tail_frac >= 0.f ? x.tail_frac : tail_fraction(x));
         if (b.attempt_log && g.tid == 0) {
           const int64_t k = st.attempts + attempts;
           if (k < b.log_cap) {
@@ -1084,7 +1115,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
         ++attempts;
         // log s feeds only the learned controller's features (an FP64 log per attempt
         // would otherwise hold the slow FP64 pipe)
-        const float f_s = learned ? clampf(safe_log(s), -8.f, 8.f) : 0.f;
+        const float f_s = learned ? log_clamped8(s) : 0.f;
         if (!ok) {
           accept = false;
           ++rejects;
@@ -1110,7 +1141,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
               f[0] = f_s;
               f[1] = s_prev;
               f[2] = s_prev2;
-              f[3] = h_prev > 0.0 ? clampf(safe_log(h / h_prev), -3.f, 3.f) : 0.f;
+              f[3] = h_prev > 0.0 ? clampf(__logf((float)h / (float)h_prev), -3.f, 3.f) : 0.f;
               f[4] = acc_prev;
               f[5] = fminf((float)numloops, 5.f);
               f[6] = clampf(lt, -30.f, 0.f);
@@ -1119,7 +1150,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
             g.sync();
             const float y = mlp_infer(g, reinterpret_cast<const unsigned char*>(b.mlp), mlp_s, mlp_s + MLP_IN);
             const float d = fminf(fmaxf(y, -1.f), 1.f);
-            const double fac = fmin(fmax(exp((double)(f_s + d)) / (double)b.mlp_target, 0.5), 4.0);
+            const double fac = (double)fminf(fmaxf(__expf(f_s + d) / b.mlp_target, 0.5f), 4.f);
             hs = (y == y) ? h * fac : accept_h(s, h, ctl);
             if (ladder) hs = ladder_step(hs, h0, false);
           } else {

@@ -141,7 +141,11 @@ __global__ void pack_kernel(const float* __restrict__ p, const float* __restrict
   for (int e = t; e < nw; e += gridDim.x * blockDim.x) {
     float v;
     if (e < MLP_H * MLP_IN) v = p[MP_W1 + e];
-    else if (e < MLP_H * MLP_IN + MLP_H * MLP_H) v = p[MP_W2 + e - MLP_H * MLP_IN];
+    else if (e < MLP_H * MLP_IN + MLP_H * MLP_H) {
+      // W2 transposed: entry k * MLP_H + j holds W2[j][k]
+      const int q = e - MLP_H * MLP_IN, k = q / MLP_H, j = q % MLP_H;
+      v = p[MP_W2 + j * MLP_H + k];
+    }
     else v = p[MP_W3 + e - MLP_H * MLP_IN - MLP_H * MLP_H];
     w[e] = __float2bfloat16_rn(v);
   }

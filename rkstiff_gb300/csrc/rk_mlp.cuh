@@ -47,8 +47,10 @@ RK_DEV float mlp_infer(const Group& g, const unsigned char* __restrict__ pk, con
   g.sync();
   for (int j = g.tid; j < MLP_H; j += g.nthr) {
     float z = b2[j];
+    // W2 is packed transposed (entry k * MLP_H + j = W2[j][k]): a warp reads 32 consecutive
+    // weights per k
 #pragma unroll 8
-    for (int k = 0; k < MLP_H; ++k) z += __bfloat162float(W2[j * MLP_H + k]) * h1[k];
+    for (int k = 0; k < MLP_H; ++k) z += __bfloat162float(W2[k * MLP_H + j]) * h1[k];
     h2[j] = tanhf(z);
   }
   g.sync();

@@ -299,32 +299,64 @@ def test_fp32_nls(golden):
     assert rel(u, g["nls256_ETD35_final"]) < 1e-4
 
 
+# (stage fraction s, a, b, g, D) of each coefficient h (a psi_1 + b psi_2 + g psi_3)(s z) / D
+# (etd35.py:157-288, etd34.py:107-149); the exponentials are marked with D = 0
+_COMB35 = [(0.25, 0, 0, 0, 0), (0.5, 0, 0, 0, 0), (0.75, 0, 0, 0, 0), (1.0, 0, 0, 0, 0),
+           (0.25, 1, 0, 0, 4), (0.25, 2, -1, 0, 8), (0.25, 0, 1, 0, 8), (0.5, 1, -1, 0, 2), (0.5, 0, 1, 0, 2),
+           (0.75, 12, -9, 0, 16), (0.75, -3, 0, 0, 8), (0.75, 0, 9, 0, 16), (1.0, -77, 59, 0, 42),
+           (1.0, 8, 0, 0, 7), (1.0, 111, -87, 0, 28), (1.0, -47, 143, 0, 84), (1.0, 1799, -3479, 1890, 2700),
+           (1.0, 1097, -467, -150, 1350), (1.0, -98, 398, -270, 225), (1.0, -313, 883, -90, 1350),
+           (1.0, 509, -2129, 1830, 2700)]
+_COMB34 = [(1.0, 0, 0, 0, 0), (0.5, 0, 0, 0, 0), (0.5, 1, 0, 0, 2), (0.5, 1, -1, 0, 2), (0.5, 0, 1, 0, 2),
+           (1.0, 1, -1, 0, 1), (1.0, 0, 1, 0, 1), (1.0, 6, -9, 4, 6), (1.0, 0, 3, -2, 3), (1.0, 0, -3, 4, 6)]
+
+
+def _psi_term_scale(comb, z, h, value):
+    """h (|a psi_1| + |b psi_2| + |g psi_3|)(s z) / D in FP64 (the value itself for the
+    exponentials): the magnitude the combination is formed from."""
+    s, a, b, g, D = comb
+    if D == 0:
+        return np.abs(value)
+    x = s * z
+    with np.errstate(all="ignore"):
+        em1 = np.expm1(x)
+        p1 = em1 / x
+        p2 = 2 * (em1 - x) / x**2
+        p3 = 6 * (em1 - x - x**2 / 2) / x**3
+    return h * (abs(a) * np.abs(p1) + abs(b) * np.abs(p2) + abs(g) * np.abs(p3)) / D
+
+
 @pytest.mark.parametrize("method", ["ETD35", "ETD5", "ETD34", "ETD4"])
 @pytest.mark.parametrize("h", [1e-3, 0.1, 1.7])
 def test_fp32_coefficients_round_fp64(method, h):
     """FP32 coefficients of a real operator against the FP64 evaluation rounded to FP32 over
-    z = h lambda from -1e9 to +50 (stiff, moderate, near the modecutoff, growing modes):
-    below z = -32 evaluated in FP32 in a form without cancellation (expf, whose error of up
-    to 2 ulps carries through the exponentials' products: within 6 FP32 ulps); otherwise in
-    double-float on the FP32 pipes, within 4 FP32 ulps plus 1e-13 |z| relative for |z| >=
-    modecutoff.  The second term covers the stiffest modes, where combinations such as ETD34
-    a51 = psi1 - 1.5 psi2 + 2/3 psi3 cancel their O(h/z) parts down to O(h/z^2), by ~|z|;
-    the 48-bit double-float leaves ~1e-14 |z| relative there (FP64 itself 1e-16 |z|), on
-    coefficients of size ~h/z^2 whose contribution is below FP32 resolution."""
+    z = h lambda from -1e9 to +50 (stiff, moderate, near the modecutoff, growing modes).
+    Below z = -32 they come from the stiff form in FP32 (expf, whose error of up to 2 ulps
+    carries through the exponentials' products: within 6 FP32 ulps, plus 1e-13 |z| relative:
+    combinations such as ETD34 a51 = psi1 - 1.5 psi2 + 2/3 psi3 cancel their O(h/z) parts
+    down to O(h/z^2) by ~|z|, on coefficients whose contribution is below FP32 resolution).
+    From -32 to 80 each combination comes from its own FP32 Taylor series (or the stiff form
+    where its scaled argument is >= 9): within 4 ulps of the value or 3 ulps of the
+    combination's psi-term scale h (|a psi_1| + |b psi_2| + |g psi_3|)/D, the rounding an FP32
+    evaluation of any form leaves near a zero of the combination."""
     lam = np.concatenate([-np.logspace(-6, 9, 300), np.logspace(-6, np.log10(50.0 / h), 60), [0.0]])
     order = ETD35_ORDER if method in ("ETD35", "ETD5") else ETD34_ORDER
+    combs = _COMB35 if method in ("ETD35", "ETD5") else _COMB34
     c32 = device_coeffs(method, lam, h, nat.RK_FP32).real
     c64 = device_coeffs(method, lam, h, nat.RK_FP64).real
     r32 = c64.astype(np.float32).astype(np.float64)
     ulp = np.spacing(np.abs(r32).astype(np.float32)).astype(np.float64)
-    zmag = np.maximum(1.0, np.abs(h * lam))
+    z = h * lam
+    zmag = np.maximum(1.0, np.abs(z))
     # below the modecutoff both precisions use small-mode series (FP32 storage: Taylor;
     # FP64: the reference's contour mean), whose ~1/z cancellation in combinations such as
     # a41 = (psi1 - psi2)/2 leaves them ~1e-16/|z| apart: compared on the array's scale
-    direct = np.abs(h * lam) >= 0.01
+    direct = np.abs(z) >= 0.01
     for i, name in enumerate(order):
-        ulps = np.where(h * lam < -32.0, 6.0, 4.0)
-        bad = direct & (np.abs(c32[i] - r32[i]) > ulps * ulp[i] + 1e-13 * zmag * np.abs(r32[i]) + 1e-37)
+        scale = _psi_term_scale(combs[i], z, h, c64[i])
+        ulp_s = np.spacing(np.abs(scale).astype(np.float32)).astype(np.float64)
+        tol = np.where(z < -32.0, 6.0 * ulp[i], 4.0 * ulp[i] + 3.0 * ulp_s) + 1e-13 * zmag * np.abs(r32[i]) + 1e-37
+        bad = direct & (np.abs(c32[i] - r32[i]) > tol)
         assert not np.any(bad), (method, h, name, lam[bad][:3], c32[i][bad][:3], r32[i][bad][:3])
         small = ~direct
         assert np.max(np.abs(c32[i][small] - c64[i][small])) <= 1e-6 * np.max(np.abs(c64[i])), (method, h, name)
