@@ -112,7 +112,7 @@ struct Ctx {
   cx<T>* fb;
   double* red;
   const cx<T>* tw;   // global table of RK_TW_N twiddles
-  const cx<T>* tws;  // compile-time path: shared-memory table of 2^LOGN twiddles
+  const cx<T>* tws;  // compile-time path: the block's twiddle rows in shared memory
   CtlF cf;           // FP32 controller constants (FP32 working precision)
   bool want_tail;    // the attempt's pass over unew also forms the tail-energy fraction
   mutable float tail_frac;  // that fraction (-1: not formed by the attempt)
@@ -128,46 +128,41 @@ struct Ctx {
 //
 // u*ux on a real grid: inverse FFT of n points, the product written as reals by the last
 // inverse pass, forward FFT of n/2 points, split into the n/2+1 rfft modes times c.
-// The FFT buffers and the twiddle table arrive as byte offsets into the kernel's dynamic
-// shared memory and are rebuilt from it here, so that the compiler knows they address shared
-// memory inside this out-of-line function (pointer arguments would be generic).
+// The FFT buffers and the twiddle rows (fill_twiddle_rows) arrive as byte offsets into the
+// kernel's dynamic shared memory and are rebuilt from it here, so that the compiler knows
+// they address shared memory inside this out-of-line function (pointer arguments would be
+// generic).  The split's W_n^k: FP32 from row 1 of the last pass times W_R^q (one rounding
+// more than the table entry); FP64 from the global table `tw`, exactly as before.
 template <class T, int LOGN>
-__device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off, uint32_t tws_off, T c,
-                                      cx<T>* __restrict__ out) {
+__device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off, uint32_t tws_off,
+                                      const cx<T>* __restrict__ tw, T c, cx<T>* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   cx<T>* fa = reinterpret_cast<cx<T>*>(smem + fa_off);
   cx<T>* fb = reinterpret_cast<cx<T>*>(smem + fb_off);
-  const cx<T>* tws = reinterpret_cast<const cx<T>*>(smem + tws_off);
+  const cx<T>* tab = reinterpret_cast<const cx<T>*>(smem + tws_off);
   constexpr int n = 1 << LOGN, M = n >> 1;
   // last inverse pass writes the real product u*ux; the forward transform of length n/2
   // reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
-  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [](cx<T>* y, int idx, int, cx<T> v) {
+  cx<T>* w = fft_rows<T, LOGN, 0, true>(g, fa, fb, tab, [](cx<T>* y, int idx, int, cx<T> v) {
     reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
   });
   cx<T>* other = (w == fa) ? fb : fa;
-  cx<T>* F = fft_ct<T, LOGN - 1, false, LOGN>(g, w, other, tws, StoreY<T>());
+  cx<T>* F = fft_half_rows<T, LOGN, 0>(g, w, other, tab, StoreY<T>());
+  constexpr int PL = fft_passes(LOGN) - 1;
+  using L = PassInfo<LOGN, PL>;
+  const cx<T>* row1 = tab + rows_offset<LOGN, PL>();  // W_n^s, s < L::Ls
   for (int k = g.tid; k <= M; k += g.nthr) {
     cx<T> Fk = F[fpad(k == M ? 0 : k)];
     cx<T> Fm = conj(F[fpad(k == 0 ? 0 : M - k)]);
     cx<T> Fe = (Fk + Fm) * T(0.5);
     cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-    cx<T> W = Fe + (k == M ? cx<T>{T(-1), T(0)} : tws[fpad(k)]) * Fo;
+    cx<T> wk;
+    if constexpr (sizeof(T) == sizeof(double)) wk = tw[k * (RK_TW_N >> LOGN)];
+    else wk = mul_wr<T, L::R>(row1[k & (L::Ls - 1)], k / L::Ls);
+    cx<T> W = Fe + (k == M ? cx<T>{T(-1), T(0)} : wk) * Fo;
     out[k] = W * c;
   }
   g.sync();
-}
-
-// i c |v|^2 v on a complex grid: inverse FFT, the pointwise product in the last inverse
-// pass, forward FFT writing the n modes.
-template <class T, int LOGN>
-__device__ __noinline__ void nls_core(Group g, cx<T>* fa, cx<T>* fb, const cx<T>* tws, T c,
-                                      cx<T>* __restrict__ out) {
-  cx<T>* w = fft_ct<T, LOGN, true, LOGN>(g, fa, fb, tws, [c](cx<T>* y, int, int pidx, cx<T> v) {
-    T a2 = (v.x * v.x + v.y * v.y) * c;
-    y[pidx] = cx<T>{-a2 * v.y, a2 * v.x};
-  });
-  cx<T>* other = (w == fa) ? fb : fa;
-  fft_ct<T, LOGN, false, LOGN>(g, w, other, tws, [out](cx<T>*, int idx, int, cx<T> v) { out[idx] = v; });
 }
 
 template <class T, class CT, int LOGN, class KF>
@@ -217,7 +212,8 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
       auto off = [](const void* q) {
         return (uint32_t)(reinterpret_cast<const unsigned char*>(q) - smem);
       };
-      uux_core<T, LOGN>(g, off(x.fa), off(x.fb), off(x.tws), x.nl_c, out);
+      uux_core<T, LOGN>(g, off(x.fa), off(x.fb), off(x.tws), sizeof(T) == sizeof(double) ? x.tw : nullptr,
+                        x.nl_c, out);
       return;
     } else {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
@@ -230,11 +226,11 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
       g.sync();
       F = fft_group<T, false>(g, other, z, x.logn - 1, x.tw);
     }
-    // rfft of the real product from the length-n/2 transform (split formula);
-    // exp(-2 pi i k/n) from the n-point shared table (compile-time path) or the global one
-    const cx<T>* twu = LOGN > 0 ? x.tws : x.tw;
-    const int tws = LOGN > 0 ? 1 : (RK_TW_N >> x.logn);
-    auto TP = [](int c) { return LOGN > 0 ? fpad(c) : c; };  // the shared table is padded
+    // rfft of the real product from the length-n/2 transform (split formula), with
+    // exp(-2 pi i k/n) from the global table (runtime-size path; the compile-time path
+    // returned above)
+    const cx<T>* twu = x.tw;
+    const int tws = RK_TW_N >> x.logn;
     for (int k0 = g.tid; k0 <= M; k0 += PK * g.nthr) {
       cx<T> W[PK];
 #pragma unroll
@@ -245,7 +241,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
         cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
         cx<T> Fe = (Fk + Fm) * T(0.5);
         cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[TP(k * tws)]) * Fo;
+        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[k * tws]) * Fo;
       }
 #pragma unroll
       for (int q = 0; q < PK; ++q) {
@@ -277,9 +273,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     }
     g.sync();
     const T c = x.nl_c;
-    if constexpr (LOGN > 0) {
-      nls_core<T, LOGN>(g, x.fa, x.fb, x.tws, c, out);
-    } else {
+    {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
       for (int t = g.tid; t < n; t += g.nthr) {
@@ -1243,8 +1237,8 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
 // A block holds blockDim.x / gthreads independent groups; each group owns one slice of
 // shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction
 // scratch, the work-item slot, then (PLACE > 0) the instance arrays (group_smem bytes in
-// all).  Compile-time-size kernels put a block-wide table of the 2^LOGN twiddles after the
-// group slices.  A one-warp group synchronises with __syncwarp, a multi-warp group with a
+// all).  Compile-time-size kernels put the block's twiddle rows (fill_twiddle_rows) after
+// the group slices.  A one-warp group synchronises with __syncwarp, a multi-warp group with a
 // named barrier (one per group), a block-wide group with __syncthreads.
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const int32_t* __restrict__ order,
@@ -1256,8 +1250,7 @@ __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const 
   cx<T>* tws = nullptr;
   if constexpr (LOGN > 0) {
     tws = reinterpret_cast<cx<T>*>(smem + (size_t)ngroups * group_smem);
-    const cx<T>* tw = reinterpret_cast<const cx<T>*>(b.twiddle);
-    for (int j = threadIdx.x; j < (1 << LOGN); j += blockDim.x) tws[fpad(j)] = tw[j * (RK_TW_N >> LOGN)];
+    fill_twiddle_rows<T, LOGN>(tws, reinterpret_cast<const cx<T>*>(b.twiddle), threadIdx.x, blockDim.x);
     __syncthreads();
   }
   unsigned char* base = smem + (size_t)gi * group_smem;

@@ -278,3 +278,175 @@ struct StoreY {
 };
 
 }  // namespace rk
+
+namespace rk {
+
+// ---------------------------------------------------------------------------------
+// Twiddle rows.  The compile-time u*ux transforms read their twiddles from one table per
+// block: for every pass p (radix R, sub-length Ls > 1) of the 2^LOGN-point transform the rows
+// T_p[(r - 1) Ls + k] = W_{R Ls}^{r k} (r = 1..R-1, k < Ls).  A pass reads T_p + k at the
+// compile-time offsets (r - 1) Ls: consecutive lanes (consecutive k) hit consecutive
+// entries, no bank conflicts and no per-twiddle index arithmetic.  The forward transform of
+// 2^(LOGN-1) points needs W_{Rf Lsf}^{r k} = W_{Ri Lsi}^{(alpha r)(beta k)} with alpha beta
+// = Ri Lsi / (Rf Lsf): a compile-time map onto a pass of the table (smallest beta, so the
+// reads stay contiguous where they can).  The split formula's W_n^k, k < n/2, is row 1 of the
+// last pass (W_n^s, s < Ls_last) times W_R^q, q = k / Ls_last (q < 4).  The table holds the
+// values of the global table (same angles, same rounding), so the transforms are bitwise
+// those of the full padded table it replaces, and it is smaller (n (R_last - 1)/R_last + a
+// few entries against n + n/16).
+// ---------------------------------------------------------------------------------
+template <int LOGN, int P>
+struct PassInfo {
+  static constexpr int LGR = PassRadix<LOGN, P>::used();
+  static constexpr int DONE = PassRadix<LOGN, P>::bits_before();
+  static constexpr int R = 1 << LGR, Ls = 1 << DONE;
+  static constexpr bool last = DONE + LGR == LOGN;
+  static constexpr int rows = DONE > 0 ? (R - 1) * Ls : 0;  // table entries of this pass
+};
+
+__host__ __device__ constexpr int fft_passes(int logn) {
+  int left = logn, p = 0;
+  while (left > 0) {
+    int lg = left >= 4 ? 4 : left;
+    if (left == 6 || left == 5) lg = 3;
+    if (left == 7) lg = 4;
+    const int cap = logn - 5 < 1 ? 1 : logn - 5;
+    lg = lg > cap ? cap : lg;
+    left -= lg;
+    ++p;
+  }
+  return p;
+}
+
+// table offset of pass P's rows, and the table's size
+template <int LOGN, int P>
+__host__ __device__ constexpr int rows_offset() {
+  if constexpr (P == 0) return 0;
+  else return rows_offset<LOGN, P - 1>() + PassInfo<LOGN, P - 1>::rows;
+}
+template <int LOGN>
+__host__ __device__ constexpr int twiddle_rows() {
+  if constexpr (LOGN <= 0) return 0;  // runtime-size kernels keep no rows
+  else return rows_offset<LOGN, fft_passes(LOGN) - 1>() + PassInfo<LOGN, fft_passes(LOGN) - 1>::rows;
+}
+
+// fill the rows of the 2^LOGN-point transform from the global table of RK_TW_N twiddles
+template <class T, int LOGN, int P = 0>
+RK_DEV void fill_twiddle_rows(cx<T>* tab, const cx<T>* __restrict__ tw, int tid, int nthr) {
+  using I = PassInfo<LOGN, P>;
+  if constexpr (I::rows > 0) {
+    cx<T>* t = tab + rows_offset<LOGN, P>();
+    for (int e = tid; e < I::rows; e += nthr) {
+      const int r = e / I::Ls + 1, k = e % I::Ls;
+      t[e] = tw[(r * k) * (RK_TW_N / (I::R * I::Ls))];
+    }
+  }
+  if constexpr (!I::last) fill_twiddle_rows<T, LOGN, P + 1>(tab, tw, tid, nthr);
+}
+
+// map of forward pass PF of the 2^(LOGN-1) transform onto the rows: PI * 10000 + alpha * 100
+// + beta, -1 if no pass serves it
+template <int LOGN, int PF, int PI = 1>
+__host__ __device__ constexpr int fwd_row_map() {
+  using F = PassInfo<LOGN - 1, PF>;
+  if constexpr (PI >= fft_passes(LOGN)) {
+    return -1;
+  } else {
+    using I = PassInfo<LOGN, PI>;
+    int best = -1;
+    if (I::Ls > 1 && (I::R * I::Ls) % (F::R * F::Ls) == 0) {
+      const int a = (I::R * I::Ls) / (F::R * F::Ls);
+      for (int beta = 1; beta <= a; beta *= 2) {
+        const int alpha = a / beta;
+        if (alpha * (F::R - 1) <= I::R - 1 && beta * (F::Ls - 1) <= I::Ls - 1) {
+          best = PI * 10000 + alpha * 100 + beta;
+          break;
+        }
+      }
+    }
+    const int rest = fwd_row_map<LOGN, PF, PI + 1>();
+    if (best < 0) return rest;
+    if (rest < 0) return best;
+    return (best % 100) <= (rest % 100) ? best : rest;
+  }
+}
+
+// One Stockham pass (as stockham_pass) with its twiddles W^{r k} at rows[(ALPHA r - 1) LSI +
+// BETA k]
+template <class T, int LOGN, int LGR, int LGLS, bool INV, int ALPHA, int BETA, int LSI, class Store>
+RK_DEV void stockham_pass_rows(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ rows,
+                               Store store) {
+  constexpr int N = 1 << LOGN, R = 1 << LGR, Ls = 1 << LGLS, NB = N / R;
+  for (int i = g.tid; i < NB; i += g.nthr) {
+    const int k = i & (Ls - 1);
+    const cx<T>* xi = x + fpad(i);
+    cx<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = xi[r * NB + ((r * NB) >> 4)];
+    if constexpr (Ls > 1) {
+      const cx<T>* tk = rows + BETA * k;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tk, (ALPHA * r - 1) * LSI);
+    }
+    dft_reg<T, R, INV>(v);
+    const int j = ((i - k) << LGR) + k;
+    const int pj = fpad(j);
+#pragma unroll
+    for (int r = 0; r < R; ++r) store(j + r * Ls, pj + r * Ls + ((r * Ls) >> 4), v[r]);
+  }
+}
+
+// the 2^LOGN-point transform (sign INV) through its own rows
+template <class T, int LOGN, int P, bool INV, class FinalStore>
+RK_DEV cx<T>* fft_rows(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tab, FinalStore fin) {
+  using I = PassInfo<LOGN, P>;
+  const cx<T>* rows = tab + rows_offset<LOGN, P>();
+  if constexpr (I::last) {
+    stockham_pass_rows<T, LOGN, I::LGR, I::DONE, INV, 1, 1, I::Ls>(
+        g, x, rows, [&](int idx, int pidx, cx<T> v) { fin(y, idx, pidx, v); });
+    g.sync();
+    return y;
+  } else {
+    stockham_pass_rows<T, LOGN, I::LGR, I::DONE, INV, 1, 1, I::Ls>(g, x, rows,
+                                                                   [&](int, int pidx, cx<T> v) { y[pidx] = v; });
+    g.sync();
+    return fft_rows<T, LOGN, P + 1, INV>(g, y, x, tab, fin);
+  }
+}
+
+// the forward 2^(LOGN-1)-point transform through the rows of the 2^LOGN-point one
+template <class T, int LOGN, int P, class FinalStore>
+RK_DEV cx<T>* fft_half_rows(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tab, FinalStore fin) {
+  using F = PassInfo<LOGN - 1, P>;
+  constexpr int MAP = F::Ls > 1 ? fwd_row_map<LOGN, P>() : 10101;
+  static_assert(MAP >= 0, "no pass of the twiddle rows serves this forward pass");
+  constexpr int PI = MAP / 10000, ALPHA = (MAP / 100) % 100, BETA = MAP % 100;
+  const cx<T>* rows = tab + rows_offset<LOGN, PI>();
+  if constexpr (F::last) {
+    stockham_pass_rows<T, LOGN - 1, F::LGR, F::DONE, false, ALPHA, BETA, PassInfo<LOGN, PI>::Ls>(
+        g, x, rows, [&](int idx, int pidx, cx<T> v) { fin(y, idx, pidx, v); });
+    g.sync();
+    return y;
+  } else {
+    stockham_pass_rows<T, LOGN - 1, F::LGR, F::DONE, false, ALPHA, BETA, PassInfo<LOGN, PI>::Ls>(
+        g, x, rows, [&](int, int pidx, cx<T> v) { y[pidx] = v; });
+    g.sync();
+    return fft_half_rows<T, LOGN, P + 1>(g, y, x, tab, fin);
+  }
+}
+
+// v W_R^q, q < 4, R the radix of the last pass (4 or 8)
+template <class T, int R>
+RK_DEV cx<T> mul_wr(cx<T> v, int q) {
+  static_assert(R == 4 || R == 8, "split twiddles need a last pass of radix 4 or 8");
+  if constexpr (R == 4) {
+    return q == 0 ? v : mul_mi(v);
+  } else {
+    const T h = T(0.7071067811865476);
+    if (q == 0) return v;
+    if (q == 2) return mul_mi(v);
+    return v * (q == 1 ? cx<T>{h, -h} : cx<T>{-h, -h});
+  }
+}
+
+}  // namespace rk
