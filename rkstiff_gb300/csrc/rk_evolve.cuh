@@ -151,16 +151,34 @@ __device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off,
   constexpr int PL = fft_passes(LOGN) - 1;
   using L = PassInfo<LOGN, PL>;
   const cx<T>* row1 = tab + rows_offset<LOGN, PL>();  // W_n^s, s < L::Ls
-  for (int k = g.tid; k <= M; k += g.nthr) {
-    cx<T> Fk = F[fpad(k == M ? 0 : k)];
-    cx<T> Fm = conj(F[fpad(k == 0 ? 0 : M - k)]);
-    cx<T> Fe = (Fk + Fm) * T(0.5);
-    cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-    cx<T> wk;
-    if constexpr (sizeof(T) == sizeof(double)) wk = tw[k * (RK_TW_N >> LOGN)];
-    else wk = mul_wr<T, L::R>(row1[k & (L::Ls - 1)], k / L::Ls);
-    cx<T> W = Fe + (k == M ? cx<T>{T(-1), T(0)} : wk) * Fo;
-    out[k] = W * c;
+  // Split, rfft mode k from F[k] and conj(F[M - k]): the modes k and M - k read the same two
+  // values, so one thread forms both (units q = 0 .. M/2 - 1: modes q and M - q; unit 0
+  // also the self-paired mode M/2), with W_n^(M - q) = -conj(W_n^q) in FP32.  M/2 units
+  // divide evenly over any group of up to M/2 threads.
+  auto mode = [&](int k, cx<T> Fk, cx<T> Fm, cx<T> wk) {
+    const cx<T> Fe = (Fk + Fm) * T(0.5);
+    const cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+    out[k] = (Fe + wk * Fo) * c;
+  };
+  for (int q = g.tid; q < M / 2; q += g.nthr) {
+    const cx<T> a = F[fpad(q)];
+    const cx<T> b = F[fpad(q == 0 ? 0 : M - q)];
+    cx<T> wq, wm;
+    if constexpr (sizeof(T) == sizeof(double)) {
+      wq = tw[q * (RK_TW_N >> LOGN)];
+      wm = q == 0 ? cx<T>{T(-1), T(0)} : tw[(M - q) * (RK_TW_N >> LOGN)];
+    } else {
+      wq = mul_wr<T, L::R>(row1[q & (L::Ls - 1)], q / L::Ls);
+      wm = cx<T>{-wq.x, wq.y};
+    }
+    mode(q, a, conj(b), wq);
+    mode(q == 0 ? M : M - q, b, conj(a), wm);
+    if (q == 0) {
+      const cx<T> h = F[fpad(M / 2)];
+      cx<T> wh{T(0), T(-1)};  // W_n^(n/4) = -i
+      if constexpr (sizeof(T) == sizeof(double)) wh = tw[(M / 2) * (RK_TW_N >> LOGN)];
+      mode(M / 2, h, conj(h), wh);
+    }
   }
   g.sync();
 }
@@ -179,31 +197,23 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     const int n = LOGN > 0 ? (1 << LOGN) : x.n, M = n >> 1;
     const T inv_n = T(1) / T(n);
     cx<T>* Z = x.fa;
-    // the stage values of PK modes are formed (all their loads issued) before any store
-    constexpr int PK = 1;
-    for (int j0 = g.tid; j0 <= M; j0 += PK * g.nthr) {
-      cx<T> kv[PK];
-      T kxv[PK];
-#pragma unroll
-      for (int q = 0; q < PK; ++q) {
-        const int j = j0 + q * g.nthr;
-        const bool in = j <= M;
-        kv[q] = in ? kf(j) : cx<T>{T(0), T(0)};
-        kxv[q] = in ? x.kx[j] : T(0);
+    auto pack = [&](int j, cx<T> kv, T kxv) {
+      cx<T> A = kv * inv_n;
+      cx<T> B = mul_i(kv) * (kxv * inv_n);
+      if (j == 0 || j == M) {
+        A.y = T(0);
+        B.y = T(0);
       }
-#pragma unroll
-      for (int q = 0; q < PK; ++q) {
-        const int j = j0 + q * g.nthr;
-        if (j > M) break;
-        cx<T> A = kv[q] * inv_n;
-        cx<T> B = mul_i(kv[q]) * (kxv[q] * inv_n);
-        if (j == 0 || j == M) {
-          A.y = T(0);
-          B.y = T(0);
-        }
-        Z[P(j)] = cx<T>{A.x - B.y, A.y + B.x};
-        if (j > 0 && j < M) Z[P(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
-      }
+      Z[P(j)] = cx<T>{A.x - B.y, A.y + B.x};
+      if (j > 0 && j < M) Z[P(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
+    };
+    // modes 0 .. M-1 over the group, the Nyquist mode M with mode 0: for a group of up to M
+    // threads M is a multiple of its size, so no thread runs an extra iteration for one mode
+    for (int j = g.tid; j < M; j += g.nthr) {
+      const cx<T> kv = kf(j);
+      const T kxv = x.kx[j];
+      if (j == 0) pack(M, kf(M), x.kx[M]);
+      pack(j, kv, kxv);
     }
     g.sync();
     cx<T>* F;
@@ -231,24 +241,12 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     // returned above)
     const cx<T>* twu = x.tw;
     const int tws = RK_TW_N >> x.logn;
-    for (int k0 = g.tid; k0 <= M; k0 += PK * g.nthr) {
-      cx<T> W[PK];
-#pragma unroll
-      for (int q = 0; q < PK; ++q) {
-        const int k = k0 + q * g.nthr;
-        if (k > M) break;
-        cx<T> Fk = F[P(k == M ? 0 : k)];
-        cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
-        cx<T> Fe = (Fk + Fm) * T(0.5);
-        cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-        W[q] = Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[k * tws]) * Fo;
-      }
-#pragma unroll
-      for (int q = 0; q < PK; ++q) {
-        const int k = k0 + q * g.nthr;
-        if (k > M) break;
-        out[k] = W[q] * x.nl_c;
-      }
+    for (int k = g.tid; k <= M; k += g.nthr) {
+      cx<T> Fk = F[P(k == M ? 0 : k)];
+      cx<T> Fm = conj(F[P(k == 0 ? 0 : M - k)]);
+      cx<T> Fe = (Fk + Fm) * T(0.5);
+      cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+      out[k] = (Fe + (k == M ? cx<T>{T(-1), T(0)} : twu[k * tws]) * Fo) * x.nl_c;
     }
     g.sync();
   } else if constexpr (LOGN > 0) {
@@ -572,7 +570,7 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const CtlF
   x.g.sync();  // the last transform has released the buffer
   float mx = 0.f;
   bool nan = false;
-  for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+  auto one = [&](int j) {
     const cx<T> v = kf(j);
     const cx<T> e = ef(j);
     x.unew[j] = v;
@@ -581,6 +579,13 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const CtlF
     else mx = fmaxf(mx, a2);
     park[2 * j] = a2;
     park[2 * j + 1] = e.x * e.x + e.y * e.y;
+  };
+  // an odd mode count (a real grid's n/2 + 1) puts its last mode with mode 0, so that the
+  // group's threads run the same number of iterations over these global loads
+  const int odd = x.m & 1;
+  for (int j = x.g.tid; j < x.m - odd; j += x.g.nthr) {
+    if (odd && j == 0) one(x.m - 1);
+    one(j);
   }
   const float maxu = group_max_nan_f(x.g, x.red, mx, nan);
   // NaN keeps every comparison false, as in the reference
@@ -896,40 +901,42 @@ enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
 // replaces after them.  Kept out of line: the learned controller's ladder uses them, the
 // plain path does not, and their state would otherwise sit in registers through every
 // transform.
+// The helpers take the instance's slab pointer and return their results by value: a
+// reference to the kernel's rk_batch parameter or to a field of the stepping context would
+// give those objects an address, and every later read of them in the stepping loop would then
+// come from local memory instead of registers or the parameter bank.
 template <class T, class CT, int METHOD>
-RK_DEV unsigned char* slab_of(const rk_batch& b, int inst) {
-  return reinterpret_cast<unsigned char*>(b.slab) + b.slab_off[inst];
-}
-template <class T, class CT, int METHOD>
-RK_DEV CT* coef_block0(const rk_batch& b, int inst, int mp) {
+RK_DEV CT* coef_block0(unsigned char* slab, int mp) {
   constexpr int NV = Traits<METHOD>::NN + (unew_in_n2(METHOD) ? 1 : 2);
   constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
-  cx<T>* gsl = reinterpret_cast<cx<T>*>(slab_of<T, CT, METHOD>(b, inst));
+  cx<T>* gsl = reinterpret_cast<cx<T>*>(slab);
   return reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NV * mp) + KXW * mp);
 }
 template <class T, class CT, int METHOD>
-RK_DEV double* coef_tags(const rk_batch& b, int inst, int m, int nblk) {
+RK_DEV double* coef_tags(unsigned char* slab, int m, int nblk) {
   const int64_t bytes = slab_bytes(METHOD, sizeof(T) == 8 ? RK_FP64 : RK_FP32, sizeof(CT) == 2 * sizeof(T), m, nblk);
-  return reinterpret_cast<double*>(slab_of<T, CT, METHOD>(b, inst) + bytes - RK_TAG_BYTES);
+  return reinterpret_cast<double*>(slab + bytes - RK_TAG_BYTES);
 }
 
-// Points C at the block whose tag is h; returns false then.  Otherwise takes the next block in
-// turn, tags it with h (after a barrier: every thread has read the tags before one changes
-// them) and returns true -- the caller rebuilds that block, and compute_coeffs' closing
-// barrier publishes the new tag.
+template <class CT>
+struct CoefPick {
+  CT* C;      // the block to use
+  double hc;  // coef_block: 1 if the caller rebuilds C, else 0; coef_block_resume: h_coeff
+};
+
+// The block whose tag is h (rebuild 0).  Otherwise takes the next block in turn, tags it with
+// h (after a barrier: every thread has read the tags before one changes them) and returns it
+// with rebuild 1 -- the caller rebuilds that block, and compute_coeffs' closing barrier
+// publishes the new tag.
 template <class T, class CT, int METHOD>
-__device__ __noinline__ bool coef_block(const rk_batch& b, int inst, Group g, int mp, int m, int nblk, double h,
-                                        CT*& C) {
-  double* tags = coef_tags<T, CT, METHOD>(b, inst, m, nblk);
-  CT* const C0 = coef_block0<T, CT, METHOD>(b, inst, mp);
+__device__ __noinline__ CoefPick<CT> coef_block(unsigned char* slab, Group g, int mp, int m, int nblk, double h) {
+  double* tags = coef_tags<T, CT, METHOD>(slab, m, nblk);
+  CT* const C0 = coef_block0<T, CT, METHOD>(slab, mp);
   const int64_t blk = (int64_t)Traits<METHOD>::NC * mp;
   int hit = -1;
   for (int i = 0; i < nblk; ++i)
     if (tags[i] == h) hit = i;
-  if (hit >= 0) {
-    C = C0 + hit * blk;
-    return false;
-  }
+  if (hit >= 0) return CoefPick<CT>{C0 + hit * blk, 0.0};
   long long* next = reinterpret_cast<long long*>(tags + RK_COEF_BLOCKS_MAX);
   const int victim = (int)(*next % nblk);
   g.sync();
@@ -937,29 +944,27 @@ __device__ __noinline__ bool coef_block(const rk_batch& b, int inst, Group g, in
     tags[victim] = h;
     *next = victim + 1;
   }
-  C = C0 + victim * blk;
-  return true;
+  return CoefPick<CT>{C0 + victim * blk, 1.0};
 }
 
 // At the start of a launch: h_coeff NaN (a fresh record, or a noalloc call) invalidates every
-// tag; otherwise C points at the block tagged h_coeff, and if none is, h_coeff is dropped.
+// tag; otherwise the block tagged h_coeff, and if none is, h_coeff is dropped (C unchanged).
 template <class T, class CT, int METHOD>
-__device__ __noinline__ double coef_block_resume(const rk_batch& b, int inst, Group g, int mp, int m, int nblk,
-                                                 double hc, CT*& C) {
-  double* tags = coef_tags<T, CT, METHOD>(b, inst, m, nblk);
+__device__ __noinline__ CoefPick<CT> coef_block_resume(unsigned char* slab, Group g, int mp, int m, int nblk,
+                                                       double hc, CT* C) {
+  double* tags = coef_tags<T, CT, METHOD>(slab, m, nblk);
   if (hc != hc) {
     g.sync();
     if (g.tid < RK_COEF_BLOCKS_MAX) tags[g.tid] = __longlong_as_double(0x7ff8000000000000ULL);
     if (g.tid == 0) *reinterpret_cast<long long*>(tags + RK_COEF_BLOCKS_MAX) = 0;
     g.sync();
-    return hc;
+    return CoefPick<CT>{C, hc};
   }
   int found = -1;
   for (int i = 0; i < nblk; ++i)
     if (tags[i] == hc) found = i;
-  if (found < 0) return __longlong_as_double(0x7ff8000000000000ULL);  // rebuild before the first attempt
-  C = coef_block0<T, CT, METHOD>(b, inst, mp) + found * (int64_t)Traits<METHOD>::NC * mp;
-  return hc;
+  if (found < 0) return CoefPick<CT>{C, __longlong_as_double(0x7ff8000000000000ULL)};  // rebuild first
+  return CoefPick<CT>{coef_block0<T, CT, METHOD>(slab, mp) + found * (int64_t)Traits<METHOD>::NC * mp, hc};
 }
 
 // u <- unew after an accepted step.  With the new state in N2's array the two arrays swap
@@ -1044,7 +1049,12 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   // Coefficient blocks (b.coef_blocks > 1): see coef_block / coef_block_resume
   const int nblk =
       (!Tr::ADAPT || PLACE == PL_SMEM_ALL || b.coef_blocks <= 1) ? 1 : min(b.coef_blocks, RK_COEF_BLOCKS_MAX);
-  if (nblk > 1) hc = coef_block_resume<T, CT, METHOD>(b, inst, g, x.mp, x.m, nblk, hc, x.C);
+  if (nblk > 1) {
+    const CoefPick<CT> r =
+        coef_block_resume<T, CT, METHOD>(reinterpret_cast<unsigned char*>(gsl), g, x.mp, x.m, nblk, hc, x.C);
+    x.C = r.C;
+    hc = r.hc;
+  }
   // the learned controller's step-size ladder starts at the instance's first step size
   const bool ladder = Tr::ADAPT && b.ladder != 0 && b.mlp != nullptr;
   double h0 = st.reserved_d;
@@ -1072,7 +1082,13 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
       double hs = h;
       for (;;) {
         if (h != hc) {  // exact compare, as the reference's _update_coeffs
-          if (nblk <= 1 || coef_block<T, CT, METHOD>(b, inst, g, x.mp, x.m, nblk, h, x.C)) {
+          bool rebuild = true;
+          if (nblk > 1) {
+            const CoefPick<CT> r = coef_block<T, CT, METHOD>(reinterpret_cast<unsigned char*>(gsl), g, x.mp, x.m, nblk, h);
+            x.C = r.C;
+            rebuild = r.hc != 0.0;
+          }
+          if (rebuild) {
             compute_coeffs<T, CT, S, METHOD>(x, h, ec);
             ++coeff_updates;
           }

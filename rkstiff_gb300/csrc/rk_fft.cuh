@@ -371,6 +371,28 @@ __host__ __device__ constexpr int fwd_row_map() {
   }
 }
 
+// The R - 1 twiddles t_r = W^{r k} (r = 1..R-1) of one butterfly, t_r at tk[(ALPHA r - 1) LSI].
+// FP64 reads every one.  FP32 reads t_1..t_3 and t_4, t_8, t_12 and forms the others as one
+// product t_{4a + b} = t_{4a} t_b (b = 1..3): 6 shared-memory reads instead of 15 for radix
+// 16, 4 instead of 7 for radix 8, each product within ~1.5 FP32 ulps of the table value.
+// The reads were a fifth of the transforms' shared-memory wavefronts.
+template <class T, int R, bool INV, int ALPHA, int LSI>
+RK_DEV void load_twiddles(const cx<T>* __restrict__ tk, cx<T>* t) {
+  if constexpr (sizeof(T) == sizeof(double) || R <= 4) {
+#pragma unroll
+    for (int r = 1; r < R; ++r) t[r] = twiddle<T, INV>(tk, (ALPHA * r - 1) * LSI);
+  } else {
+#pragma unroll
+    for (int r = 1; r < 4; ++r) t[r] = twiddle<T, INV>(tk, (ALPHA * r - 1) * LSI);
+#pragma unroll
+    for (int a = 4; a < R; a += 4) {
+      t[a] = twiddle<T, INV>(tk, (ALPHA * a - 1) * LSI);
+#pragma unroll
+      for (int b = 1; b < 4; ++b) t[a + b] = t[a] * t[b];
+    }
+  }
+}
+
 // One Stockham pass (as stockham_pass) with its twiddles W^{r k} at rows[(ALPHA r - 1) LSI +
 // BETA k]
 template <class T, int LOGN, int LGR, int LGLS, bool INV, int ALPHA, int BETA, int LSI, class Store>
@@ -384,9 +406,10 @@ RK_DEV void stockham_pass_rows(const Group& g, const cx<T>* __restrict__ x, cons
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = xi[r * NB + ((r * NB) >> 4)];
     if constexpr (Ls > 1) {
-      const cx<T>* tk = rows + BETA * k;
+      cx<T> t[R];
+      load_twiddles<T, R, INV, ALPHA, LSI>(rows + BETA * k, t);
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tk, (ALPHA * r - 1) * LSI);
+      for (int r = 1; r < R; ++r) v[r] = v[r] * t[r];
     }
     dft_reg<T, R, INV>(v);
     const int j = ((i - k) << LGR) + k;
