@@ -4,11 +4,13 @@ Each class (instances sharing one grid size) runs as its own kernel, concurrentl
 other classes.  The tuner first takes the classes one at a time, each on its own: the
 class's instances (up to ``per_class`` of them) as a one-class ensemble, every candidate
 (threads per instance group, groups per block, scratch placement) timed over a short span
-of simulated time (best of ``reps`` + 1 runs).  Alone, a class's kernel is what is timed;
-inside the mix the slowest class sets the wall time and hides the others' candidates.  The
-finalists within 5% of a class's best are timed again over twice the span, in alternating
-order, and a class whose runner-up stays within 3% is settled by runs of the whole ensemble
-(greedy, class by class), where the classes share the GPU as in the real launch.  Results
+of simulated time (best of ``reps`` + 1 runs, CUDA-event time).  Alone, a class's kernel is
+what is timed; inside the mix the slowest class sets the wall time and hides the others'
+candidates.  The finalists within 8% of a class's best are timed again over twice the span,
+in alternating order, and a class whose runner-up stays within 8% is settled by runs of the
+whole ensemble over twice the span (greedy, class by class), where the classes share the GPU
+as in the real launch: alone, shapes of one class that differ by 5% came out equal in the
+mix, and the mix is what a launch runs.  Results
 are cached per (device, method, precision, operator kind, nonlinearity, grid-size mix) for
 the process and can be saved to / loaded from a JSON file.
 """
@@ -17,7 +19,6 @@ from __future__ import annotations
 
 import json
 import os
-import time
 from typing import Dict, Optional, Sequence, Tuple
 
 import numpy as np
@@ -65,16 +66,20 @@ def _install(eng: DiagEnsemble, shapes) -> None:
 def _rate(sub: DiagEnsemble, u0: torch.Tensor, span: float, h: float, reps: int) -> Optional[float]:
     u = torch.empty_like(u0)
     best = None
+    stream = torch.cuda.current_stream(sub.device)
     for _ in range(reps + 1):
         u.copy_(u0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(sub.device)
-        t0 = time.perf_counter()
+        a.record(stream)
         try:
             st = sub.evolve(u, 0.0, span, h)
         except nat.NativeError:
             return None  # a shape that does not fit this size
+        b.record(stream)
         torch.cuda.synchronize(sub.device)
-        rate = float(np.sum(sub.ms * st["steps"])) / (time.perf_counter() - t0)
+        rate = float(np.sum(sub.ms * st["steps"])) / (a.elapsed_time(b) * 1e-3)
         best = rate if best is None else max(best, rate)
     return best
 
@@ -117,10 +122,10 @@ def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequ
                     rates[(t, gr, p)] = r
         if not rates:
             raise RuntimeError(f"no launch shape fits grid size {n}")
-        # finalists (within 5% of the best, at most three) timed again over twice the span,
+        # finalists (within 8% of the best, at most three) timed again over twice the span,
         # best of five, in alternating order, so that run-to-run noise does not pick the shape
         top = sorted(rates.items(), key=lambda kv: -kv[1])
-        final = [c for c, r in top[:3] if r >= 0.95 * top[0][1]]
+        final = [c for c, r in top[:3] if r >= 0.92 * top[0][1]]
         refined = {c: 0.0 for c in final}
         if len(final) > 1:
             for rep in range(2 * reps):
@@ -129,24 +134,24 @@ def tune(eng: DiagEnsemble, u0s: Sequence, lin_ops: Sequence, kxs: Optional[Sequ
                     refined[c] = max(refined[c], _rate(sub, u0, 2 * span, h, 0) or 0.0)
         ranked = sorted(final, key=lambda c: -refined[c]) if len(final) > 1 else final
         chosen.append(ranked[0])
-        runner_up.append(ranked[1] if len(ranked) > 1 and refined[ranked[1]] >= 0.97 * refined[ranked[0]] else None)
+        runner_up.append(ranked[1] if len(ranked) > 1 and refined[ranked[1]] >= 0.92 * refined[ranked[0]] else None)
         best = ranked[0]
         report[int(n)] = {"threads": best[0], "groups": best[1], "place": best[2],
                           "rates": {f"{a}x{b}/{p}": v for (a, b, p), v in rates.items()}}
     # The classes run concurrently in the real launch: where a class's runner-up came within
-    # 3% of its choice alone, the whole ensemble decides between them (greedy, one class at
-    # a time, best of reps + 1 mixed runs over the span).
+    # 8% of its choice alone, the whole ensemble decides between them (greedy, one class at
+    # a time, best of reps + 1 mixed runs over twice the span).
     if len(eng.class_n) > 1 and any(r is not None for r in runner_up):
         u_all = eng.pack_u(list(u0s))
         _install(eng, chosen)
-        base = _rate(eng, u_all, span, h, reps) or 0.0
+        base = _rate(eng, u_all, 2 * span, h, reps) or 0.0
         for c, alt in enumerate(runner_up):
             if alt is None:
                 continue
             trial = list(chosen)
             trial[c] = alt
             _install(eng, trial)
-            r = _rate(eng, u_all, span, h, reps) or 0.0
+            r = _rate(eng, u_all, 2 * span, h, reps) or 0.0
             if r > base:
                 chosen, base = trial, r
                 n = int(eng.class_n[c])

@@ -122,17 +122,136 @@ struct Ctx {
 // ---------------------------------------------------------------------------------
 // built-in nonlinearities: out[j] = N(k)[j] with k[j] = kf(j)
 // ---------------------------------------------------------------------------------
-// Transform part of the built-in nonlinearities for a compile-time grid size, kept out of
-// line so that its fully unrolled passes exist once per kernel rather than once per stage.
-// The packed spectrum is in fa (padded); the result goes to out[0 .. m).
+// The u*ux packing fused with the first pass (radix R0, no twiddles) of the inverse
+// n-point transform.  The packed spectrum is Z = A + iB with A = k/n and B = i kx k/n the
+// Hermitian spectra of u and u_x: Z[j] = (A.x - B.y, A.y + B.x) and Z[n-j] = (A.x + B.y, B.x -
+// A.y) for 0 < j < n/2, the imaginary parts of A and B dropped at j = 0 and n/2 (as numpy's
+// irfft drops them).  Butterfly c of the pass needs Z[c + r NB0], r < R0: the rows r < R0/2
+// are modes of column c, the others mirror images of the modes of column NB0 - c.  A lane
+// pair holds the columns c and NB0 - c (paired_column), so each lane evaluates kf for the
+// R0/2 modes of its own column and swaps the mirror images with its partner by shuffles;
+// columns 0 and NB0/2 mirror themselves (column 0 also takes the Nyquist mode n/2).  Every
+// mode is evaluated once, and the packed spectrum never goes through shared memory.
+template <class T, int LOGN, class KF>
+RK_DEV void pack_first_pass(const Group& g, KF kf, const T* __restrict__ kx, cx<T>* __restrict__ y, T inv_n) {
+  using P0 = PassInfo<LOGN, 0>;
+  constexpr int n = 1 << LOGN, M = n / 2, R0 = P0::R, NB0 = n / R0, H = R0 / 2;
+  static_assert(P0::DONE == 0 && R0 >= 2 && NB0 % 32 == 0, "paired first pass: whole warps of butterflies");
+  auto packed = [&](int j, cx<T>& own, cx<T>& mirror) {
+    const cx<T> kv = kf(j);
+    const T kxv = kx[j];
+    cx<T> A = kv * inv_n;
+    cx<T> B = mul_i(kv) * (kxv * inv_n);
+    if (j == 0 || j == M) {
+      A.y = T(0);
+      B.y = T(0);
+    }
+    own = cx<T>{A.x - B.y, A.y + B.x};
+    mirror = cx<T>{A.x + B.y, B.x - A.y};
+  };
+  for (int tt = g.tid; tt < NB0; tt += g.nthr) {
+    const int c = paired_column(tt, NB0);
+    const bool self = (tt >> 1) == 0;  // columns 0 and NB0/2: their own mirror images
+    const bool col0 = c == 0;
+    cx<T> v[R0], mir[H], nyq{T(0), T(0)}, unused;
+#pragma unroll
+    for (int r = 0; r < H; ++r) packed(c + r * NB0, v[r], mir[r]);
+    if (col0) packed(M, nyq, unused);
+    cx<T> p[H];
+#pragma unroll
+    for (int r = 0; r < H; ++r) p[r] = shfl_pair(mir[r]);
+    // rows s >= H: Z[c + s NB0] = mirror image of mode (NB0 - c) + (R0 - 1 - s) NB0, which is
+    // the partner's mode at row R0-1-s; for column 0 mode (R0 - s) NB0 (row H: the Nyquist
+    // mode itself), for column NB0/2 its own mode at row R0-1-s
+#pragma unroll
+    for (int s = H; s < R0; ++s) {
+      const cx<T> d = (s == H) ? nyq : mir[(R0 - s) % H];
+      v[s] = !self ? p[R0 - 1 - s] : (col0 ? d : mir[R0 - 1 - s]);
+    }
+    dft_reg<T, R0, true>(v);
+#pragma unroll
+    for (int r = 0; r < R0; ++r) y[fpad(c * R0 + r)] = v[r];
+  }
+}
+
+// Last pass of the forward n/2-point transform fused with the rfft split.  Butterfly k (k <
+// NB, the pass's sub-length) produces F[k + r NB], r < Rf; rfft mode k' = k + r NB needs F[k']
+// and conj(F[n/2 - k']), and n/2 - k' = (NB - k) + (Rf - 1 - r) NB is an output of butterfly
+// NB - k: with the butterflies paired over lane pairs (paired_column) the partner's outputs
+// arrive by shuffles, and each lane writes the Rf modes of its butterfly (butterfly 0 also
+// the Nyquist mode n/2) with no pass through shared memory.
+// mode k': out = ((F + conj(Fm))/2 + W_n^k' (-i)(F - conj(Fm))/2) c.  W_n^k': FP32 from row 1
+// of the inverse transform's last pass (W_n^k, k < NB) times the constant W_n^(r NB) =
+// W_16^(8 r / Rf); FP64 from the global table `tw`.
+template <class T, int LOGN>
+RK_DEV void fwd_last_split(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ tab,
+                           const cx<T>* __restrict__ tw, T c, cx<T>* __restrict__ out) {
+  constexpr int PF = fft_passes(LOGN - 1, true) - 1;
+  using F = PassInfo<LOGN - 1, PF, true>;
+  constexpr int Rf = F::R, NB = F::Ls, M = 1 << (LOGN - 1);
+  static_assert(F::last && F::DONE > 0 && NB * Rf == M, "last forward pass");
+  static_assert(NB % 32 == 0, "paired butterflies: whole warps");
+  static_assert(Rf <= 8, "W_n^(r NB) = W_16^(8 r / Rf) needs Rf <= 8");
+  constexpr int MAP = fwd_map<LOGN, PF>();
+  static_assert(MAP >= 0, "no pass of the twiddle rows serves the last forward pass");
+  constexpr int PI = MAP / 10000, ALPHA = (MAP / 100) % 100, BETA = MAP % 100;
+  const cx<T>* rows = tab + rows_offset<LOGN, PI>();
+  constexpr int PL = fft_passes(LOGN) - 1;
+  static_assert(NB <= PassInfo<LOGN, PL>::Ls, "W_n^k, k < NB, from row 1 of the last inverse pass");
+  const cx<T>* row1 = tab + rows_offset<LOGN, PL>();
+  constexpr int TWS = RK_TW_N >> LOGN;
+  auto mode = [&](int k, cx<T> Fk, cx<T> Fm, cx<T> wk) {
+    const cx<T> Fe = (Fk + Fm) * T(0.5);
+    const cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+    out[k] = (Fe + wk * Fo) * c;
+  };
+  for (int tt = g.tid; tt < NB; tt += g.nthr) {
+    const int k = paired_column(tt, NB);
+    const bool self = (tt >> 1) == 0;
+    const bool col0 = k == 0;
+    const cx<T>* xi = x + fpad(k);
+    cx<T> v[Rf];
+#pragma unroll
+    for (int r = 0; r < Rf; ++r) v[r] = xi[r * NB + ((r * NB) >> 4)];
+    {
+      cx<T> t[Rf];
+      load_twiddles<T, Rf, false, ALPHA, PassInfo<LOGN, PI>::Ls>(rows + BETA * k, t);
+#pragma unroll
+      for (int r = 1; r < Rf; ++r) v[r] = v[r] * t[r];
+    }
+    dft_reg<T, Rf, false>(v);
+    cx<T> p[Rf];
+#pragma unroll
+    for (int r = 0; r < Rf; ++r) p[r] = shfl_pair(v[r]);
+    cx<T> wk{T(1), T(0)};
+    if constexpr (sizeof(T) == sizeof(float)) wk = row1[k];
+    static_for<Rf>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      // F[n/2 - k']: the partner's row Rf-1-r; butterfly 0: its own row (Rf - r) % Rf;
+      // butterfly NB/2: its own row Rf-1-r
+      const cx<T> fm = !self ? p[Rf - 1 - r] : (col0 ? v[(Rf - r) % Rf] : v[Rf - 1 - r]);
+      cx<T> w;
+      if constexpr (sizeof(T) == sizeof(double)) w = tw[(k + r * NB) * TWS];
+      else w = mul_w16<T, false, (8 * r) / Rf>(wk);
+      mode(k + r * NB, v[r], conj(fm), w);
+    });
+    if (col0) mode(M, v[0], conj(v[0]), cx<T>{T(-1), T(0)});
+  }
+  g.sync();
+}
+
+// Transform part of the u*ux nonlinearity for a compile-time grid size, kept out of line so
+// that its fully unrolled passes exist once per kernel rather than once per stage.
 //
-// u*ux on a real grid: inverse FFT of n points, the product written as reals by the last
-// inverse pass, forward FFT of n/2 points, split into the n/2+1 rfft modes times c.
+// On entry fb holds the output of the inverse transform's first pass (pack_first_pass).  The
+// remaining inverse passes run, the last one writing the real product u*ux; the forward
+// transform of n/2 points reads it as complex pairs (real t at 2*fpad(t/2) + t%2); its last
+// pass is fused with the split into the n/2+1 rfft modes times c (fwd_last_split), which
+// writes out[0 .. n/2].
 // The FFT buffers and the twiddle rows (fill_twiddle_rows) arrive as byte offsets into the
 // kernel's dynamic shared memory and are rebuilt from it here, so that the compiler knows
 // they address shared memory inside this out-of-line function (pointer arguments would be
-// generic).  The split's W_n^k: FP32 from row 1 of the last pass times W_R^q (one rounding
-// more than the table entry); FP64 from the global table `tw`, exactly as before.
+// generic).
 template <class T, int LOGN>
 __device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off, uint32_t tws_off,
                                       const cx<T>* __restrict__ tw, T c, cx<T>* __restrict__ out) {
@@ -140,47 +259,61 @@ __device__ __noinline__ void uux_core(Group g, uint32_t fa_off, uint32_t fb_off,
   cx<T>* fa = reinterpret_cast<cx<T>*>(smem + fa_off);
   cx<T>* fb = reinterpret_cast<cx<T>*>(smem + fb_off);
   const cx<T>* tab = reinterpret_cast<const cx<T>*>(smem + tws_off);
-  constexpr int n = 1 << LOGN, M = n >> 1;
-  // last inverse pass writes the real product u*ux; the forward transform of length n/2
-  // reads it as complex pairs (real t at 2*fpad(t/2) + t%2)
-  cx<T>* w = fft_rows<T, LOGN, 0, true>(g, fa, fb, tab, [](cx<T>* y, int idx, int, cx<T> v) {
+  constexpr bool FUSED = uux_fused(LOGN);
+  auto prod = [](cx<T>* y, int idx, int, cx<T> v) {
     reinterpret_cast<T*>(y)[2 * fpad(idx >> 1) + (idx & 1)] = v.x * v.y;
-  });
-  cx<T>* other = (w == fa) ? fb : fa;
-  cx<T>* F = fft_half_rows<T, LOGN, 0>(g, w, other, tab, StoreY<T>());
-  constexpr int PL = fft_passes(LOGN) - 1;
-  using L = PassInfo<LOGN, PL>;
-  const cx<T>* row1 = tab + rows_offset<LOGN, PL>();  // W_n^s, s < L::Ls
-  // Split, rfft mode k from F[k] and conj(F[M - k]): the modes k and M - k read the same two
-  // values, so one thread forms both (units q = 0 .. M/2 - 1: modes q and M - q; unit 0
-  // also the self-paired mode M/2), with W_n^(M - q) = -conj(W_n^q) in FP32.  M/2 units
-  // divide evenly over any group of up to M/2 threads.
-  auto mode = [&](int k, cx<T> Fk, cx<T> Fm, cx<T> wk) {
-    const cx<T> Fe = (Fk + Fm) * T(0.5);
-    const cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
-    out[k] = (Fe + wk * Fo) * c;
   };
-  for (int q = g.tid; q < M / 2; q += g.nthr) {
-    const cx<T> a = F[fpad(q)];
-    const cx<T> b = F[fpad(q == 0 ? 0 : M - q)];
-    cx<T> wq, wm;
-    if constexpr (sizeof(T) == sizeof(double)) {
-      wq = tw[q * (RK_TW_N >> LOGN)];
-      wm = q == 0 ? cx<T>{T(-1), T(0)} : tw[(M - q) * (RK_TW_N >> LOGN)];
-    } else {
-      wq = mul_wr<T, L::R>(row1[q & (L::Ls - 1)], q / L::Ls);
-      wm = cx<T>{-wq.x, wq.y};
+  // fused: pass 0 ran in pack_first_pass (output in fb); unfused: the packed spectrum is in fa
+  cx<T>* w = FUSED ? fft_rows<T, LOGN, 1, true>(g, fb, fa, tab, prod) : fft_rows<T, LOGN, 0, true>(g, fa, fb, tab, prod);
+  cx<T>* other = (w == fa) ? fb : fa;
+  const cx<T>* x = fft_half_rows_to_last<T, LOGN, 0>(g, w, other, tab);
+  if constexpr (FUSED) {
+    fwd_last_split<T, LOGN>(g, x, tab, tw, c, out);
+  } else {
+    // last forward pass into the other buffer, then the split: rfft mode k from F[k] and
+    // conj(F[M - k]); the modes k and M - k read the same two values, so one thread forms
+    // both (units q = 0 .. M/2 - 1: modes q and M - q; unit 0 also the self-paired mode M/2),
+    // with W_n^(M - q) = -conj(W_n^q) in FP32.  M/2 units divide evenly over any group of up
+    // to M/2 threads.
+    constexpr int M = 1 << (LOGN - 1);
+    constexpr int PF = fft_passes(LOGN - 1, true) - 1;
+    using F = PassInfo<LOGN - 1, PF, true>;
+    constexpr int MAP = fwd_map<LOGN, PF>();
+    constexpr int PI = MAP / 10000, ALPHA = (MAP / 100) % 100, BETA = MAP % 100;
+    cx<T>* Fb = (x == fa) ? fb : fa;
+    stockham_pass_rows<T, LOGN - 1, F::LGR, F::DONE, false, ALPHA, BETA, PassInfo<LOGN, PI>::Ls>(
+        g, x, tab + rows_offset<LOGN, PI>(), [&](int, int pidx, cx<T> v) { Fb[pidx] = v; });
+    g.sync();
+    constexpr int PL = fft_passes(LOGN) - 1;
+    using L = PassInfo<LOGN, PL>;
+    const cx<T>* row1 = tab + rows_offset<LOGN, PL>();  // W_n^s, s < L::Ls
+    auto mode = [&](int k, cx<T> Fk, cx<T> Fm, cx<T> wk) {
+      const cx<T> Fe = (Fk + Fm) * T(0.5);
+      const cx<T> Fo = mul_mi(Fk - Fm) * T(0.5);
+      out[k] = (Fe + wk * Fo) * c;
+    };
+    for (int q = g.tid; q < M / 2; q += g.nthr) {
+      const cx<T> a = Fb[fpad(q)];
+      const cx<T> b = Fb[fpad(q == 0 ? 0 : M - q)];
+      cx<T> wq, wm;
+      if constexpr (sizeof(T) == sizeof(double)) {
+        wq = tw[q * (RK_TW_N >> LOGN)];
+        wm = q == 0 ? cx<T>{T(-1), T(0)} : tw[(M - q) * (RK_TW_N >> LOGN)];
+      } else {
+        wq = mul_wr<T, L::R>(row1[q & (L::Ls - 1)], q / L::Ls);
+        wm = cx<T>{-wq.x, wq.y};
+      }
+      mode(q, a, conj(b), wq);
+      mode(q == 0 ? M : M - q, b, conj(a), wm);
+      if (q == 0) {
+        const cx<T> h = Fb[fpad(M / 2)];
+        cx<T> wh{T(0), T(-1)};  // W_n^(n/4) = -i
+        if constexpr (sizeof(T) == sizeof(double)) wh = tw[(M / 2) * (RK_TW_N >> LOGN)];
+        mode(M / 2, h, conj(h), wh);
+      }
     }
-    mode(q, a, conj(b), wq);
-    mode(q == 0 ? M : M - q, b, conj(a), wm);
-    if (q == 0) {
-      const cx<T> h = F[fpad(M / 2)];
-      cx<T> wh{T(0), T(-1)};  // W_n^(n/4) = -i
-      if constexpr (sizeof(T) == sizeof(double)) wh = tw[(M / 2) * (RK_TW_N >> LOGN)];
-      mode(M / 2, h, conj(h), wh);
-    }
+    g.sync();
   }
-  g.sync();
 }
 
 template <class T, class CT, int LOGN, class KF>
@@ -196,6 +329,39 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     // parts of the DC and Nyquist bins, so they are dropped here too.
     const int n = LOGN > 0 ? (1 << LOGN) : x.n, M = n >> 1;
     const T inv_n = T(1) / T(n);
+    if constexpr (LOGN > 0) {
+      extern __shared__ __align__(16) unsigned char smem[];
+      auto off = [](const void* q) {
+        return (uint32_t)(reinterpret_cast<const unsigned char*>(q) - smem);
+      };
+if constexpr (uux_fused(LOGN)) {
+        pack_first_pass<T, LOGN>(g, kf, x.kx, x.fb, inv_n);
+      } else {
+        cx<T>* Z = x.fa;
+        auto pack = [&](int j, cx<T> kv, T kxv) {
+          cx<T> A = kv * inv_n;
+          cx<T> B = mul_i(kv) * (kxv * inv_n);
+          if (j == 0 || j == M) {
+            A.y = T(0);
+            B.y = T(0);
+          }
+          Z[fpad(j)] = cx<T>{A.x - B.y, A.y + B.x};
+          if (j > 0 && j < M) Z[fpad(n - j)] = cx<T>{A.x + B.y, B.x - A.y};
+        };
+        // modes 0 .. M-1 over the group, the Nyquist mode M with mode 0: for a group of up to
+        // M threads M is a multiple of its size, so no thread runs an extra iteration for it
+        for (int j = g.tid; j < M; j += g.nthr) {
+          const cx<T> kv = kf(j);
+          const T kxv = x.kx[j];
+          if (j == 0) pack(M, kf(M), x.kx[M]);
+          pack(j, kv, kxv);
+        }
+      }
+      g.sync();
+      uux_core<T, LOGN>(g, off(x.fa), off(x.fb), off(x.tws), sizeof(T) == sizeof(double) ? x.tw : nullptr,
+                        x.nl_c, out);
+      return;
+    }
     cx<T>* Z = x.fa;
     auto pack = [&](int j, cx<T> kv, T kxv) {
       cx<T> A = kv * inv_n;
@@ -217,15 +383,7 @@ RK_DEV void nl_eval(const Ctx<T, CT, LOGN>& x, KF kf, cx<T>* __restrict__ out) {
     }
     g.sync();
     cx<T>* F;
-    if constexpr (LOGN > 0) {
-      extern __shared__ __align__(16) unsigned char smem[];
-      auto off = [](const void* q) {
-        return (uint32_t)(reinterpret_cast<const unsigned char*>(q) - smem);
-      };
-      uux_core<T, LOGN>(g, off(x.fa), off(x.fb), off(x.tws), sizeof(T) == sizeof(double) ? x.tw : nullptr,
-                        x.nl_c, out);
-      return;
-    } else {
+    {
       cx<T>* z = fft_group<T, true>(g, x.fa, x.fb, x.logn, x.tw);
       cx<T>* other = (z == x.fa) ? x.fb : x.fa;
       T* w = reinterpret_cast<T*>(other);

@@ -6,6 +6,8 @@
 // table tw[k] = exp(-2*pi*i*k/RK_TW_N) (FP64-accurate, stored in the working precision).
 #pragma once
 
+#include <utility>
+
 #include "rk_common.cuh"
 
 namespace rk {
@@ -183,23 +185,43 @@ RK_DEV void dft_reg(cx<T>* v) {
   }
 }
 
-// radix of pass p for a size-2^LOGN transform: 16 while >= 4 bits remain, then the rest,
-// preferring 8+8 over 16+4 / 16+2 splits of the last 6/5 bits; the radix is capped so that
-// a pass has at least 32 butterflies (N / R >= 32), which keeps every lane of a one-warp
-// group busy on the small transforms (n = 128, 256) instead of half or a quarter of them.
-template <int LOGN, int P>
+// Per grid size n = 2^logn of a u*ux kernel: whether the packing is fused with the inverse
+// transform's first pass and the split with the forward transform's last pass
+// (pack_first_pass, fwd_last_split; both exchange values between lane pairs by shuffles
+// instead of a pass through shared memory), and with it the pass plans.  Chosen by timing
+// each grid-size class of the KS ensemble workload (about 1000 instances, ETD35 FP32, tf =
+// 100) on a GB300, ms per class:
+//   n = 2048  unfused, inverse 16.16.8, forward 16.8.8     104.4   (fused, 8.16.16 / 8.16.8: 109.1)
+//   n = 1024  fused,   inverse 8.16.8,  forward 8.8.8       55.5   (unfused, 16.8.8 / 16.8.4: 57.2)
+//   n = 512   unfused, inverse 16.8.4,  forward 8.8.4       31.0   (fused, 8.8.8 / 8.8.4: 33.2)
+//   n = 256   fused,   inverse 8.8.4,   forward 4.4.4.2     18.3   (unfused: 20.1)
+// A fused pass runs one lane per butterfly and evaluates several modes per lane; where that
+// leaves lanes of the group idle or puts radix-16 passes on half the lanes, the unfused form
+// is faster.
+__host__ __device__ constexpr bool uux_fused(int logn) { return logn == 8 || logn == 10; }
+
+// log2 of the radix of pass p of a size-2^logn transform (fwd: the forward n/2-point
+// transform of a kernel of 2n points): 16 while >= 4 bits remain, preferring 8+8 over 16+4 /
+// 16+2 splits of the last 6/5 bits; at most 8 for the first pass of a fused kernel's
+// transforms (the paired first pass holds two columns' worth of values per lane pair); every
+// radix is capped so that a pass has at least 32 butterflies (N / R >= 32), which keeps
+// every lane of a one-warp group busy on the small transforms (n = 128, 256) instead of half
+// or a quarter of them.
+__host__ __device__ constexpr int pass_pick(int logn, int p, int left, bool fwd) {
+  int lg = left >= 4 ? 4 : left;
+  if (left == 6 || left == 5) lg = 3;
+  if (left == 7) lg = 4;
+  if (p == 0 && lg > 3 && uux_fused(fwd ? logn + 1 : logn)) lg = 3;
+  const int cap = logn - 5 < 1 ? 1 : logn - 5;
+  return lg > cap ? cap : lg;
+}
+
+template <int LOGN, int P, bool FWD = false>
 struct PassRadix {
-  __host__ __device__ static constexpr int pick(int left) {
-    int lg = left >= 4 ? 4 : left;
-    if (left == 6 || left == 5) lg = 3;
-    if (left == 7) lg = 4;
-    const int cap = LOGN - 5 < 1 ? 1 : LOGN - 5;
-    return lg > cap ? cap : lg;
-  }
   __host__ __device__ static constexpr int used() {
     int left = LOGN, lg = 0;
     for (int q = 0; q <= P; ++q) {
-      lg = pick(left);
+      lg = pass_pick(LOGN, q, left, FWD);
       left -= lg;
     }
     return lg;
@@ -207,70 +229,13 @@ struct PassRadix {
   __host__ __device__ static constexpr int bits_before() {
     int left = LOGN, done = 0;
     for (int q = 0; q < P; ++q) {
-      const int lg = pick(left);
+      const int lg = pass_pick(LOGN, q, left, FWD);
       left -= lg;
       done += lg;
     }
     return done;
   }
 };
-
-// One Stockham pass of radix R = 2^LGR at sub-length Ls = 2^LGLS over N = 2^LOGN points.
-// `store(idx, pidx, value)` receives each output with its unpadded index and its padded
-// position fpad(idx).  With power-of-two R, Ls and NB the padded positions of a butterfly's
-// inputs i + r NB and outputs j + r Ls are its base position plus compile-time offsets
-// (fpad(a + b) = fpad(a) + b + (b >> 4) for these b), so each load and store needs no
-// index arithmetic of its own.
-template <class T, int LOGN, int LGR, int LGLS, bool INV, int TWLOG, class Store>
-RK_DEV void stockham_pass(const Group& g, const cx<T>* __restrict__ x, const cx<T>* __restrict__ tw, Store store) {
-  constexpr int N = 1 << LOGN, R = 1 << LGR, Ls = 1 << LGLS, NB = N / R;
-  constexpr int TWS = (1 << TWLOG) >> (LGLS + LGR);  // table stride of W_{R Ls}
-  for (int i = g.tid; i < NB; i += g.nthr) {
-    const int k = i & (Ls - 1);
-    const cx<T>* xi = x + fpad(i);
-    cx<T> v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = xi[r * NB + ((r * NB) >> 4)];
-    if constexpr (Ls > 1) {
-      // twiddle tables of 2^TWLOG <= 4096 entries live in shared memory at padded
-      // positions (strided reads would otherwise fall into a few banks)
-#pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = v[r] * twiddle<T, INV>(tw, fpad(r * k * TWS));
-    }
-    dft_reg<T, R, INV>(v);
-    const int j = ((i - k) << LGR) + k;
-    const int pj = fpad(j);
-#pragma unroll
-    for (int r = 0; r < R; ++r) store(j + r * Ls, pj + r * Ls + ((r * Ls) >> 4), v[r]);
-  }
-}
-
-template <class T, int LOGN, int P, bool INV, int TWLOG, class FinalStore>
-RK_DEV cx<T>* fft_ct_passes(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tw, FinalStore fin) {
-  constexpr int LGR = PassRadix<LOGN, P>::used();
-  constexpr int DONE = PassRadix<LOGN, P>::bits_before();
-  if constexpr (DONE + LGR == LOGN) {
-    // final pass: outputs go to fin(y, index, value); y is the buffer not being read
-    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int idx, int pidx, cx<T> v) { fin(y, idx, pidx, v); });
-    g.sync();
-    return y;
-  } else {
-    stockham_pass<T, LOGN, LGR, DONE, INV, TWLOG>(g, x, tw, [&](int, int pidx, cx<T> v) { y[pidx] = v; });
-    g.sync();
-    return fft_ct_passes<T, LOGN, P + 1, INV, TWLOG>(g, y, x, tw, fin);
-  }
-}
-
-// FFT of 2^LOGN points held in `a` at padded positions fpad(i) (`b` is scratch of the same
-// size), with `tw` a table of the 2^TWLOG twiddles exp(-2 pi i k/2^TWLOG), TWLOG >= LOGN,
-// stored at padded positions fpad(k).
-// The final pass hands every output to fin(y, index, padded index, value), where y is the
-// buffer that pass does not read and `index` the unpadded output index; returns y.  All group threads
-// call.
-template <class T, int LOGN, bool INV, int TWLOG, class FinalStore>
-RK_DEV cx<T>* fft_ct(const Group& g, cx<T>* a, cx<T>* b, const cx<T>* tw, FinalStore fin) {
-  return fft_ct_passes<T, LOGN, 0, INV, TWLOG>(g, a, b, tw, fin);
-}
 
 template <class T>
 struct StoreY {
@@ -295,24 +260,19 @@ namespace rk {
 // those of the full padded table it replaces, and it is smaller (n (R_last - 1)/R_last + a
 // few entries against n + n/16).
 // ---------------------------------------------------------------------------------
-template <int LOGN, int P>
+template <int LOGN, int P, bool FWD = false>
 struct PassInfo {
-  static constexpr int LGR = PassRadix<LOGN, P>::used();
-  static constexpr int DONE = PassRadix<LOGN, P>::bits_before();
+  static constexpr int LGR = PassRadix<LOGN, P, FWD>::used();
+  static constexpr int DONE = PassRadix<LOGN, P, FWD>::bits_before();
   static constexpr int R = 1 << LGR, Ls = 1 << DONE;
   static constexpr bool last = DONE + LGR == LOGN;
   static constexpr int rows = DONE > 0 ? (R - 1) * Ls : 0;  // table entries of this pass
 };
 
-__host__ __device__ constexpr int fft_passes(int logn) {
+__host__ __device__ constexpr int fft_passes(int logn, bool fwd = false) {
   int left = logn, p = 0;
   while (left > 0) {
-    int lg = left >= 4 ? 4 : left;
-    if (left == 6 || left == 5) lg = 3;
-    if (left == 7) lg = 4;
-    const int cap = logn - 5 < 1 ? 1 : logn - 5;
-    lg = lg > cap ? cap : lg;
-    left -= lg;
+    left -= pass_pick(logn, p, left, fwd);
     ++p;
   }
   return p;
@@ -348,7 +308,7 @@ RK_DEV void fill_twiddle_rows(cx<T>* tab, const cx<T>* __restrict__ tw, int tid,
 // + beta, -1 if no pass serves it
 template <int LOGN, int PF, int PI = 1>
 __host__ __device__ constexpr int fwd_row_map() {
-  using F = PassInfo<LOGN - 1, PF>;
+  using F = PassInfo<LOGN - 1, PF, true>;
   if constexpr (PI >= fft_passes(LOGN)) {
     return -1;
   } else {
@@ -437,32 +397,64 @@ RK_DEV cx<T>* fft_rows(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tab, Fin
   }
 }
 
-// the forward 2^(LOGN-1)-point transform through the rows of the 2^LOGN-point one
-template <class T, int LOGN, int P, class FinalStore>
-RK_DEV cx<T>* fft_half_rows(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tab, FinalStore fin) {
-  using F = PassInfo<LOGN - 1, P>;
-  constexpr int MAP = F::Ls > 1 ? fwd_row_map<LOGN, P>() : 10101;
-  static_assert(MAP >= 0, "no pass of the twiddle rows serves this forward pass");
-  constexpr int PI = MAP / 10000, ALPHA = (MAP / 100) % 100, BETA = MAP % 100;
-  const cx<T>* rows = tab + rows_offset<LOGN, PI>();
+// Which rows serve forward pass P of the 2^(LOGN-1)-point transform: (pass of the rows,
+// ALPHA, BETA) packed as fwd_row_map returns them; the first pass has no twiddles.
+template <int LOGN, int P>
+__host__ __device__ constexpr int fwd_map() {
+  return PassInfo<LOGN - 1, P, true>::Ls > 1 ? fwd_row_map<LOGN, P>() : 10101;
+}
+
+// Forward 2^(LOGN-1)-point transform through the rows of the 2^LOGN-point one, every pass
+// but the last; returns the buffer that holds the last pass's input.
+template <class T, int LOGN, int P>
+RK_DEV cx<T>* fft_half_rows_to_last(const Group& g, cx<T>* x, cx<T>* y, const cx<T>* tab) {
+  using F = PassInfo<LOGN - 1, P, true>;
   if constexpr (F::last) {
-    stockham_pass_rows<T, LOGN - 1, F::LGR, F::DONE, false, ALPHA, BETA, PassInfo<LOGN, PI>::Ls>(
-        g, x, rows, [&](int idx, int pidx, cx<T> v) { fin(y, idx, pidx, v); });
-    g.sync();
-    return y;
+    return x;
   } else {
+    constexpr int MAP = fwd_map<LOGN, P>();
+    static_assert(MAP >= 0, "no pass of the twiddle rows serves this forward pass");
+    constexpr int PI = MAP / 10000, ALPHA = (MAP / 100) % 100, BETA = MAP % 100;
+    const cx<T>* rows = tab + rows_offset<LOGN, PI>();
     stockham_pass_rows<T, LOGN - 1, F::LGR, F::DONE, false, ALPHA, BETA, PassInfo<LOGN, PI>::Ls>(
         g, x, rows, [&](int, int pidx, cx<T> v) { y[pidx] = v; });
     g.sync();
-    return fft_half_rows<T, LOGN, P + 1>(g, y, x, tab, fin);
+    return fft_half_rows_to_last<T, LOGN, P + 1>(g, y, x, tab);
   }
+}
+
+// value of a complex pair from the lane whose index differs in bit 0
+template <class T>
+RK_DEV cx<T> shfl_pair(cx<T> v) {
+  return cx<T>{__shfl_xor_sync(0xffffffffu, v.x, 1), __shfl_xor_sync(0xffffffffu, v.y, 1)};
+}
+
+// Paired columns of a pass with NB butterflies (NB a multiple of 32): lane pair (2q, 2q+1)
+// takes the columns q and NB - q (q = 0: 0 and NB/2), whose values are each other's mirror
+// images in a Hermitian-symmetric spectrum.  Both lanes of a pair run the same iterations of
+// a loop over tt < NB, and so do all lanes of a warp, so shfl_pair is safe inside it.
+RK_DEV int paired_column(int tt, int nb) {
+  const int unit = tt >> 1;
+  return (tt & 1) == 0 ? unit : (unit == 0 ? nb / 2 : nb - unit);
+}
+
+// compile-time loop: f(std::integral_constant<int, r>) for r = 0 .. N-1
+template <int N, class F, int... R>
+RK_DEV void static_for_impl(F&& f, std::integer_sequence<int, R...>) {
+  (f(std::integral_constant<int, R>{}), ...);
+}
+template <int N, class F>
+RK_DEV void static_for(F&& f) {
+  static_for_impl<N>(f, std::make_integer_sequence<int, N>{});
 }
 
 // v W_R^q, q < 4, R the radix of the last pass (4 or 8)
 template <class T, int R>
 RK_DEV cx<T> mul_wr(cx<T> v, int q) {
-  static_assert(R == 4 || R == 8, "split twiddles need a last pass of radix 4 or 8");
-  if constexpr (R == 4) {
+  static_assert(R == 4 || R == 8 || R == 16, "split twiddles need a last pass of radix 4, 8 or 16");
+  if constexpr (R == 16) {
+    return q == 0 ? v : q == 1 ? mul_w16<T, false, 1>(v) : q == 2 ? mul_w16<T, false, 2>(v) : mul_w16<T, false, 3>(v);
+  } else if constexpr (R == 4) {
     return q == 0 ? v : mul_mi(v);
   } else {
     const T h = T(0.7071067811865476);
