@@ -342,19 +342,21 @@ RK_DEV SerScale ser_scale(float xf, float xl) {
   return s;
 }
 
-template <int A, int B, int G, int D>
+// SH: the table is a copy in shared memory (plain loads), else the global one (__ldg)
+template <int A, int B, int G, int D, bool SH>
 RK_DEV float ser_comb(const float* __restrict__ tab, int row, const SerScale& s, float h) {
   if (s.big) return stiff_comb<A, B, G, D>(h, s.r, s.e);
   const float* p = tab + (row * RK_SER_NC + s.k) * RK_SER_NT;
-  float acc = __ldg(p + RK_SER_NT - 1);
+  float acc = SH ? p[RK_SER_NT - 1] : __ldg(p + RK_SER_NT - 1);
 #pragma unroll
-  for (int j = RK_SER_NT - 2; j >= 0; --j) acc = fmaf(acc, s.t, __ldg(p + j));
+  for (int j = RK_SER_NT - 2; j >= 0; --j) acc = fmaf(acc, s.t, SH ? p[j] : __ldg(p + j));
   return h * acc;
 }
 
-// layouts C35_* (ETD35, ETD5) and C34_* (ETD34, ETD4); z in [-STIFF_Z, 80]
-template <int METHOD>
-RK_DEV void series_coeffs_f32(double zd, double hd, float* o) {
+// layouts C35_* (ETD35, ETD5) and C34_* (ETD34, ETD4); z in [-STIFF_Z, 80].  `tab`: a copy
+// of the method's table in shared memory (SH) or null (the global table)
+template <int METHOD, bool SH = false>
+RK_DEV void series_coeffs_f32(double zd, double hd, float* o, const float* tab = nullptr) {
   const float zf = (float)zd, zl = (float)(zd - (double)zf), h = (float)hd;
   // The exponentials multiply u in every stage, so an error in them accumulates step after
   // step: they are formed in double-float and rounded once (one dd_exp of the smallest
@@ -366,41 +368,41 @@ RK_DEV void series_coeffs_f32(double zd, double hd, float* o) {
   if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) {
     const float q34 = 0.75f * zf, l34 = fmaf(0.75f, zf, -q34) + 0.75f * zl;  // 3z/4 as a pair
     const SerScale S14 = ser_scale(0.25f * zf, 0.25f * zl), S34 = ser_scale(q34, l34);
-    const float* T = k_ser_etd35;
+    const float* T = SH ? tab : k_ser_etd35;
     const dd e2 = e1 * e1, e3 = e2 * e1, e4 = e2 * e2;
     o[C35_E14] = e1.hi;
     o[C35_E12] = e2.hi;
     o[C35_E34] = e3.hi;
     o[C35_E] = e4.hi;
-    o[C35_A21] = ser_comb<1, 0, 0, 4>(T, 0, S14, h);
-    o[C35_A31] = ser_comb<2, -1, 0, 8>(T, 1, S14, h);
-    o[C35_A32] = ser_comb<0, 1, 0, 8>(T, 2, S14, h);
-    o[C35_A41] = ser_comb<1, -1, 0, 2>(T, 3, S12, h);
-    o[C35_A43] = ser_comb<0, 1, 0, 2>(T, 4, S12, h);
-    o[C35_A51] = ser_comb<12, -9, 0, 16>(T, 5, S34, h);
-    o[C35_A52] = ser_comb<-3, 0, 0, 8>(T, 6, S34, h);
-    o[C35_A54] = ser_comb<0, 9, 0, 16>(T, 7, S34, h);
-    o[C35_A61] = ser_comb<-77, 59, 0, 42>(T, 8, S1, h);
-    o[C35_A62] = ser_comb<8, 0, 0, 7>(T, 9, S1, h);
-    o[C35_A63] = ser_comb<111, -87, 0, 28>(T, 10, S1, h);
-    o[C35_A65] = ser_comb<-47, 143, 0, 84>(T, 11, S1, h);
-    o[C35_A71] = ser_comb<1799, -3479, 1890, 2700>(T, 12, S1, h);
-    o[C35_A73] = ser_comb<1097, -467, -150, 1350>(T, 13, S1, h);
-    o[C35_A74] = ser_comb<-98, 398, -270, 225>(T, 14, S1, h);
-    o[C35_A75] = ser_comb<-313, 883, -90, 1350>(T, 15, S1, h);
-    o[C35_A76] = ser_comb<509, -2129, 1830, 2700>(T, 16, S1, h);
+    o[C35_A21] = ser_comb<1, 0, 0, 4, SH>(T, 0, S14, h);
+    o[C35_A31] = ser_comb<2, -1, 0, 8, SH>(T, 1, S14, h);
+    o[C35_A32] = ser_comb<0, 1, 0, 8, SH>(T, 2, S14, h);
+    o[C35_A41] = ser_comb<1, -1, 0, 2, SH>(T, 3, S12, h);
+    o[C35_A43] = ser_comb<0, 1, 0, 2, SH>(T, 4, S12, h);
+    o[C35_A51] = ser_comb<12, -9, 0, 16, SH>(T, 5, S34, h);
+    o[C35_A52] = ser_comb<-3, 0, 0, 8, SH>(T, 6, S34, h);
+    o[C35_A54] = ser_comb<0, 9, 0, 16, SH>(T, 7, S34, h);
+    o[C35_A61] = ser_comb<-77, 59, 0, 42, SH>(T, 8, S1, h);
+    o[C35_A62] = ser_comb<8, 0, 0, 7, SH>(T, 9, S1, h);
+    o[C35_A63] = ser_comb<111, -87, 0, 28, SH>(T, 10, S1, h);
+    o[C35_A65] = ser_comb<-47, 143, 0, 84, SH>(T, 11, S1, h);
+    o[C35_A71] = ser_comb<1799, -3479, 1890, 2700, SH>(T, 12, S1, h);
+    o[C35_A73] = ser_comb<1097, -467, -150, 1350, SH>(T, 13, S1, h);
+    o[C35_A74] = ser_comb<-98, 398, -270, 225, SH>(T, 14, S1, h);
+    o[C35_A75] = ser_comb<-313, 883, -90, 1350, SH>(T, 15, S1, h);
+    o[C35_A76] = ser_comb<509, -2129, 1830, 2700, SH>(T, 16, S1, h);
   } else {
-    const float* T = k_ser_etd34;
+    const float* T = SH ? tab : k_ser_etd34;
     o[C34_E] = (e1 * e1).hi;
     o[C34_E2] = e1.hi;
-    o[C34_A21] = ser_comb<1, 0, 0, 2>(T, 0, S12, h);
-    o[C34_A31] = ser_comb<1, -1, 0, 2>(T, 1, S12, h);
-    o[C34_A32] = ser_comb<0, 1, 0, 2>(T, 2, S12, h);
-    o[C34_A41] = ser_comb<1, -1, 0, 1>(T, 3, S1, h);
-    o[C34_A43] = ser_comb<0, 1, 0, 1>(T, 4, S1, h);
-    o[C34_A51] = ser_comb<6, -9, 4, 6>(T, 5, S1, h);
-    o[C34_A52] = ser_comb<0, 3, -2, 3>(T, 6, S1, h);
-    o[C34_A54] = ser_comb<0, -3, 4, 6>(T, 7, S1, h);
+    o[C34_A21] = ser_comb<1, 0, 0, 2, SH>(T, 0, S12, h);
+    o[C34_A31] = ser_comb<1, -1, 0, 2, SH>(T, 1, S12, h);
+    o[C34_A32] = ser_comb<0, 1, 0, 2, SH>(T, 2, S12, h);
+    o[C34_A41] = ser_comb<1, -1, 0, 1, SH>(T, 3, S1, h);
+    o[C34_A43] = ser_comb<0, 1, 0, 1, SH>(T, 4, S1, h);
+    o[C34_A51] = ser_comb<6, -9, 4, 6, SH>(T, 5, S1, h);
+    o[C34_A52] = ser_comb<0, 3, -2, 3, SH>(T, 6, S1, h);
+    o[C34_A54] = ser_comb<0, -3, 4, 6, SH>(T, 7, S1, h);
   }
 }
 

@@ -50,7 +50,11 @@ constexpr int B_TILE = NT * KC * 4;
 constexpr int SLOT_BYTES = 2 * A_TILE;      // S or S^-1 chunk, hi and lo
 constexpr int DEP_BYTES = 2 * NCH * B_TILE;  // stage operand: NCH hi tiles, then NCH lo tiles
 constexpr int RED_BYTES = 3 * 4 * NT * 4;    // per-warp partial max, sum u^2, sum err^2
-constexpr int SMEM = 1024 + NS * SLOT_BYTES + DEP_BYTES + RED_BYTES + 2048;
+// the FP32 Taylor-series table of the method (rk_coef_series.cuh), copied to shared memory
+constexpr int SER_FLOATS = sizeof(k_ser_etd35) / sizeof(float) > sizeof(k_ser_etd34) / sizeof(float)
+                               ? (int)(sizeof(k_ser_etd35) / sizeof(float)) : (int)(sizeof(k_ser_etd34) / sizeof(float));
+constexpr int SER_BYTES = (SER_FLOATS * 4 + 127) & ~127;
+constexpr int SMEM = 1024 + NS * SLOT_BYTES + DEP_BYTES + RED_BYTES + 2048 + SER_BYTES;
 // warps 0-7: epilogues (two per tensor-memory lane quarter, one per column half), warp 8:
 // MMA issue, warp 9: TMA loads
 constexpr int EPI_WARPS = 8, EPI_THREADS = 32 * EPI_WARPS;
@@ -111,9 +115,11 @@ RK_DEV float nl_ac(float w, float x) {
 
 // FP32 coefficients of one real mode z = h lambda (layouts C35_*, C34_*, CIF_*): the stiff
 // form below z = -STIFF_Z, the combinations' FP32 Taylor tables / stiff forms up to z = 80
-// (series_coeffs_f32; IF34's exponentials in double-float), FP64 beyond.
+// (series_coeffs_f32 reading the kernel's shared-memory copy `ser` of the table: the global
+// table's lines missed the L1 left beside 198 KB of shared memory; 18.7 -> 17.6 ms for the
+// 8192-IC ETD35 batch; IF34's exponentials in double-float), FP64 beyond.
 template <int METHOD>
-RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
+RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out, const float* ser) {
   if (z < -(double)STIFF_Z) {
     stiff_coeffs_f32<METHOD>(z, h, out);
     return;
@@ -132,7 +138,7 @@ RK_DEV void mode_coeffs_f32(double z, double h, const EtdCfg& ec, float* out) {
     constexpr int NP = METHOD == RK_ETD35 ? RK_PSI35_N : RK_PSI34_N;
     constexpr int NC = METHOD == RK_ETD35 ? C35_N : C34_N;
     if (z <= 80.0) {
-      series_coeffs_f32<METHOD>(z, h, out);
+      series_coeffs_f32<METHOD, true>(z, h, out, ser);
     } else {
       double E[4], P[NP], o[NC];
       fast_real_psi(METHOD, z, h, E, P);
@@ -303,6 +309,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
   int* stiffq = running + NT;  // [NT] bit q: every row of chunk q of the instance is stiff at its h
   double* lamq = reinterpret_cast<double*>(stiffq + NT);                 // [4] largest eig of each chunk
   unsigned* needw = reinterpret_cast<unsigned*>(lamq + DM / 32);         // [2] need[] as a bit mask
+  float* ser = reinterpret_cast<float*>(ctl_area + 2048);                 // series table copy
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t col0 = (int64_t)blockIdx.x * NT;
@@ -328,6 +335,13 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
     }
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tmA);
+  }
+  if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD34) {
+    // the rebuilds' Taylor-series table, read by every non-stiff mode (published by the
+    // __syncthreads below)
+    constexpr int nf = (int)((METHOD == RK_ETD35 ? sizeof(k_ser_etd35) : sizeof(k_ser_etd34)) / sizeof(float));
+    const float* src = METHOD == RK_ETD35 ? k_ser_etd35 : k_ser_etd34;
+    for (int i = tid; i < nf; i += THREADS) ser[i] = src[i];
   }
   __syncwarp();
   if (warp == 0) {
@@ -597,7 +611,7 @@ __global__ void __launch_bounds__(THREADS, 1) eig_kernel(const __grid_constant__
               const int r = q * 32 + lane;
               float c[NCF];
               const double h = hsm[j];
-              mode_coeffs_f32<METHOD>(h * p.eig[r], h, p.ec, c);
+              mode_coeffs_f32<METHOD>(h * p.eig[r], h, p.ec, c, ser);
               float* cp = p.C + ((col0 + j) * C35_N) * DM + r;
 #pragma unroll
               for (int k = 0; k < NCF; ++k) cp[k * DM] = c[k];
