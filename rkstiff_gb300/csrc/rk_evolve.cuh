@@ -114,6 +114,7 @@ struct Ctx {
   const cx<T>* tw;   // global table of RK_TW_N twiddles
   const cx<T>* tws;  // compile-time path: the block's twiddle rows in shared memory
   CtlF cf;           // FP32 controller constants (FP32 working precision)
+  const float* ser;  // the block's shared-memory copy of the FP32 series table, or null (global)
   bool want_tail;    // the attempt's pass over unew also forms the tail-energy fraction
   mutable float tail_frac;  // that fraction (-1: not formed by the attempt)
   RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
@@ -468,7 +469,8 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
 // register budget of the stage loop.
 template <class CT, class S, int METHOD, bool FAST>
 __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const cx<double>* __restrict__ lin,
-                                                 CT* __restrict__ C, double h, EtdCfg ec) {
+                                                 CT* __restrict__ C, double h, EtdCfg ec,
+                                                 const float* __restrict__ ser = nullptr) {
   constexpr int NC = Traits<METHOD>::NC;
   if (!is_etd(METHOD)) {
     for (int j = g.tid; j < m; j += g.nthr) {
@@ -496,7 +498,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
           // each combination's own Taylor series in FP32 (series_coeffs_f32): the FP64
           // series would hold the whole warp on the 1/64-rate FP64 pipe for one small mode
           float of[NC];
-          series_coeffs_f32<METHOD>(sre(z), h, of);
+          if (ser) series_coeffs_f32<METHOD, true>(sre(z), h, of, ser);
+          else series_coeffs_f32<METHOD>(sre(z), h, of);
 #pragma unroll
           for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         } else {
@@ -522,7 +525,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
       if (zr <= 80.0) {
         // FP32 series / stiff forms per combination (series_coeffs_f32)
         float of[NC];
-        series_coeffs_f32<METHOD>(zr, h, of);
+        if (ser) series_coeffs_f32<METHOD, true>(zr, h, of, ser);
+        else series_coeffs_f32<METHOD>(zr, h, of);
 #pragma unroll
         for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         continue;
@@ -592,7 +596,7 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
 
 template <class T, class CT, class S, int METHOD, int LOGN>
 RK_DEV void compute_coeffs(const Ctx<T, CT, LOGN>& x, double h, const EtdCfg& ec) {
-  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec);
+  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, x.ser);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1135,7 +1139,8 @@ RK_DEV void accept_swap(X& x) {
 
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
-                         unsigned char* sm_slab, const cx<T>* tws, float* mlp_s, int nfft) {
+                         unsigned char* sm_slab, const cx<T>* tws, float* mlp_s, int nfft,
+                         const unsigned char* mlpw, const float* ser) {
   using Tr = Traits<METHOD>;
   Ctx<T, CT, LOGN> x;
   x.g = g;
@@ -1164,6 +1169,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
   x.cf = make_ctlf(b.ctl);
+  x.ser = ser;
   x.want_tail = false;
   x.tail_frac = -1.f;
   const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
@@ -1316,7 +1322,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
               f[7] = tail_prev >= 0.f ? clampf(lt - log10f(tail_prev + 1e-30f), -10.f, 10.f) : 0.f;
             }
             g.sync();
-            const float y = mlp_infer(g, reinterpret_cast<const unsigned char*>(b.mlp), mlp_s, mlp_s + MLP_IN);
+            const float y = mlp_infer(g, mlpw, mlp_s, mlp_s + MLP_IN);
             const float d = fminf(fmaxf(y, -1.f), 1.f);
             const double fac = (double)fminf(fmaxf(__expf(f_s + d) / b.mlp_target, 0.5f), 4.f);
             hs = (y == y) ? h * fac : accept_h(s, h, ctl);
@@ -1408,6 +1414,26 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   g.sync();
 }
 
+RK_HD constexpr size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+static_assert(sizeof(k_ser_etd35) == sizeof(float) * 17 * RK_SER_NC * RK_SER_NT, "ETD35 series table size");
+static_assert(sizeof(k_ser_etd34) == sizeof(float) * 8 * RK_SER_NC * RK_SER_NT, "ETD34 series table size");
+// floats of the FP32 coefficient series table a method's rebuilds read (0: none)
+template <class T, int METHOD>
+RK_HD constexpr int ser_table_floats() {
+  return sizeof(T) != sizeof(float) ? 0
+         : (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? 17 * RK_SER_NC * RK_SER_NT
+         : (METHOD == RK_ETD34 || METHOD == RK_ETD4) ? 8 * RK_SER_NC * RK_SER_NT : 0;
+}
+// offset of the block-wide copies (learned-controller launches) and their bytes
+template <class T, int LOGN>
+RK_HD constexpr size_t block_extra_offset(int ngroups, int group_smem) {
+  return (size_t)ngroups * group_smem + (LOGN > 0 ? align16(sizeof(cx<T>) * twiddle_rows<LOGN>()) : 0);
+}
+template <class T, int METHOD>
+RK_HD constexpr size_t learned_extra_bytes() {
+  return align16(RK_MLP_PACK_BYTES) + align16(sizeof(float) * ser_table_floats<T, METHOD>());
+}
+
 // A block holds blockDim.x / gthreads independent groups; each group owns one slice of
 // shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction
 // scratch, the work-item slot, then (PLACE > 0) the instance arrays (group_smem bytes in
@@ -1427,6 +1453,27 @@ __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const 
     fill_twiddle_rows<T, LOGN>(tws, reinterpret_cast<const cx<T>*>(b.twiddle), threadIdx.x, blockDim.x);
     __syncthreads();
   }
+  // Launches with the learned controller: the inference buffer and (FP32 ETD methods) the
+  // coefficient series table, copied once per block into shared memory after the group
+  // slices and the twiddle rows.  From global memory, the inference's weight reads and the
+  // every-attempt rebuilds' table reads missed the small L1 beside the shared memory.
+  const unsigned char* mlpw = reinterpret_cast<const unsigned char*>(b.mlp);
+  const float* ser = nullptr;
+  if (b.mlp != nullptr) {
+    unsigned char* ex = smem + block_extra_offset<T, LOGN>(ngroups, group_smem);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(b.mlp);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(ex);
+    for (int i = threadIdx.x; i < RK_MLP_PACK_BYTES / 4; i += blockDim.x) dst[i] = src[i];
+    mlpw = ex;
+    constexpr int nser = ser_table_floats<T, METHOD>();
+    if constexpr (nser > 0) {
+      float* sr = reinterpret_cast<float*>(ex + align16(RK_MLP_PACK_BYTES));
+      const float* st = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? k_ser_etd35 : k_ser_etd34;
+      for (int i = threadIdx.x; i < nser; i += blockDim.x) sr[i] = st[i];
+      ser = sr;
+    }
+    __syncthreads();
+  }
   unsigned char* base = smem + (size_t)gi * group_smem;
   cx<T>* fa = reinterpret_cast<cx<T>*>(base);
   cx<T>* fb = fa + fpad_size(nfft);
@@ -1442,7 +1489,7 @@ __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const 
     g.sync();
     if (item >= count) break;
     const int inst = order ? order[item] : item;
-    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s, nfft);
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s, nfft, mlpw, ser);
   }
 }
 

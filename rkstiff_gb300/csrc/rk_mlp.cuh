@@ -25,7 +25,10 @@ static_assert(PK_FLOATS * 4 + (MLP_H * MLP_IN + MLP_H * MLP_H + MLP_H) * 2 == RK
 constexpr int MLP_SCRATCH_FLOATS = MLP_IN + 2 * MLP_H + 40;
 
 // y = MLP(feat) with bf16 weights and FP32 accumulation, evaluated by the whole group.
-// `feat` (MLP_IN floats, raw features) and `s` (MLP_SCRATCH_FLOATS) are shared memory.
+// `feat` (MLP_IN floats, raw features) and `s` (MLP_SCRATCH_FLOATS) are shared memory; `pk`
+// is the inference buffer, normally the block's shared-memory copy of it.  The hidden layer
+// runs on every thread of the group: P = nthr / MLP_H consecutive lanes share an output, each
+// over MLP_H / P inputs, combined by shuffles (one-warp groups: two outputs per lane).
 RK_DEV float mlp_infer(const Group& g, const unsigned char* __restrict__ pk, const float* feat, float* s) {
   const float* mu = reinterpret_cast<const float*>(pk);
   const float* isd = mu + MLP_IN;
@@ -37,7 +40,7 @@ RK_DEV float mlp_infer(const Group& g, const unsigned char* __restrict__ pk, con
   const __nv_bfloat16* w3 = W2 + MLP_H * MLP_H;
   float* h1 = s;
   float* h2 = s + MLP_H;
-  float* part = s + 2 * MLP_H;
+  float* out = s + 2 * MLP_H;
   for (int j = g.tid; j < MLP_H; j += g.nthr) {
     float z = b1[j];
 #pragma unroll
@@ -45,28 +48,28 @@ RK_DEV float mlp_infer(const Group& g, const unsigned char* __restrict__ pk, con
     h1[j] = tanhf(z);
   }
   g.sync();
-  for (int j = g.tid; j < MLP_H; j += g.nthr) {
-    float z = b2[j];
-    // W2 is packed transposed (entry k * MLP_H + j = W2[j][k]): a warp reads 32 consecutive
-    // weights per k
+  // W2 is packed transposed (entry k * MLP_H + j = W2[j][k])
+  const int P = g.nthr >= 2 * MLP_H ? (g.nthr / MLP_H > 8 ? 8 : g.nthr / MLP_H) : 1;
+  const int KP = MLP_H / P;
+  for (int t = g.tid; t < MLP_H * P; t += g.nthr) {
+    const int j = t / P, p = t - j * P;
+    float z = 0.f;
 #pragma unroll 8
-    for (int k = 0; k < MLP_H; ++k) z += __bfloat162float(W2[k * MLP_H + j]) * h1[k];
-    h2[j] = tanhf(z);
+    for (int k = p * KP; k < (p + 1) * KP; ++k) z += __bfloat162float(W2[k * MLP_H + j]) * h1[k];
+    // every lane of a warp is in this iteration when P > 1 (MLP_H * P = nthr)
+    for (int o = P >> 1; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+    if (p == 0) h2[j] = tanhf(b2[j] + z);
   }
   g.sync();
-  float acc = 0.f;
-  for (int j = g.tid; j < MLP_H; j += g.nthr) acc += __bfloat162float(w3[j]) * h2[j];
+  if (g.tid < 32) {
+    float acc = 0.f;
+    for (int j = g.tid; j < MLP_H; j += 32) acc += __bfloat162float(w3[j]) * h2[j];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  const int nw = g.nthr >> 5;
-  if (nw > 1) {
-    if ((g.tid & 31) == 0) part[g.tid >> 5] = acc;
-    g.sync();
-    acc = 0.f;
-    for (int w = 0; w < nw; ++w) acc += part[w];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (g.tid == 0) out[0] = acc + b3;
   }
   g.sync();
-  return acc + b3;
+  return out[0];
 }
 
 }  // namespace rk
