@@ -190,15 +190,19 @@ RK_DEV void dft_reg(cx<T>* v) {
 // (pack_first_pass, fwd_last_split; both exchange values between lane pairs by shuffles
 // instead of a pass through shared memory), and with it the pass plans.  Chosen by timing
 // each grid-size class of the KS ensemble workload (about 1000 instances, ETD35 FP32, tf =
-// 100) on a GB300, ms per class:
-//   n = 2048  unfused, inverse 16.16.8, forward 16.8.8     104.4   (fused, 8.16.16 / 8.16.8: 109.1)
-//   n = 1024  fused,   inverse 8.16.8,  forward 8.8.8       55.5   (unfused, 16.8.8 / 16.8.4: 57.2)
-//   n = 512   unfused, inverse 16.8.4,  forward 8.8.4       31.0   (fused, 8.8.8 / 8.8.4: 33.2)
-//   n = 256   fused,   inverse 8.8.4,   forward 4.4.4.2     18.3   (unfused: 20.1)
+// 100) on a GB300, ms per class at its best launch shape:
+//   n = 2048  fused,   inverse 8.8.8.4, forward 8.8.8.2   102.1   (unfused 16.16.8 / 16.8.8:
+//             107.5; unfused 8.8.8.4: 112.5; fused 8.16.16 / 8.16.8: 107.1)
+//   n = 1024  fused,   inverse 8.16.8,  forward 8.8.8      55.5   (unfused, 16.8.8 / 16.8.4: 57.2;
+//             fused 8.8.8.2: 55.5)
+//   n = 512   unfused, inverse 16.8.4,  forward 8.8.4      31.0   (fused, 8.8.8 / 8.8.4: 33.2)
+//   n = 256   fused,   inverse 8.8.4,   forward 4.4.4.2    18.3   (unfused: 20.1)
 // A fused pass runs one lane per butterfly and evaluates several modes per lane; where that
-// leaves lanes of the group idle or puts radix-16 passes on half the lanes, the unfused form
-// is faster.
-__host__ __device__ constexpr bool uux_fused(int logn) { return logn == 8 || logn == 10; }
+// leaves lanes of the group idle (n = 512 with 128-thread groups) the unfused form is
+// faster.  At n = 2048 radix-8 passes keep every lane of a 128- or 256-thread group busy
+// (a radix-16 pass has 128 butterflies) and need fewer registers, which pays for the fourth
+// pass only together with the fused first and last passes.
+__host__ __device__ constexpr bool uux_fused(int logn) { return logn == 8 || logn == 10 || logn == 11; }
 
 // log2 of the radix of pass p of a size-2^logn transform (fwd: the forward n/2-point
 // transform of a kernel of 2n points): 16 while >= 4 bits remain, preferring 8+8 over 16+4 /
@@ -212,6 +216,7 @@ __host__ __device__ constexpr int pass_pick(int logn, int p, int left, bool fwd)
   if (left == 6 || left == 5) lg = 3;
   if (left == 7) lg = 4;
   if (p == 0 && lg > 3 && uux_fused(fwd ? logn + 1 : logn)) lg = 3;
+  if ((fwd ? logn + 1 : logn) == 11 && lg > 3) lg = 3;  // n = 2048: radix-8 passes only
   const int cap = logn - 5 < 1 ? 1 : logn - 5;
   return lg > cap ? cap : lg;
 }
