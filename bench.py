@@ -201,7 +201,7 @@ class ClockSampler:
 TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "ks_ensemble_etd35_fp32_traffic.md")
 
 
-PLACE_NAMES = {0: "global", 1: "smem-state", 2: "smem-all"}
+PLACE_NAMES = {0: "global", 1: "smem-state", 2: "smem-all", 3: "smem-u"}
 
 
 def shape_tag(n, threads, groups, place) -> str:

@@ -241,7 +241,10 @@ enum {
   RK_PLACE_AUTO = -1,
   RK_PLACE_GLOBAL = 0,     /* all arrays in the global scratch slab                       */
   RK_PLACE_SMEM_STATE = 1, /* u, unew and stage arrays in shared memory, coefficients global */
-  RK_PLACE_SMEM_ALL = 2    /* all arrays in shared memory (coefficients rebuilt per launch) */
+  RK_PLACE_SMEM_ALL = 2,   /* all arrays in shared memory (coefficients rebuilt per launch) */
+  RK_PLACE_SMEM_U = 3      /* u and the new-state array in shared memory, the other stage
+                              arrays and the coefficients in the global slab (compile-time
+                              ETD35 kernels, n = 256 .. 2048, only)                          */
 };
 
 /* ABI version and last error message (thread-local). */

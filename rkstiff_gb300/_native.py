@@ -26,7 +26,7 @@ RK_ST_ITER_CAP, RK_ST_SNAP_FULL, RK_ST_STEP_DONE, RK_ST_BAD_SIZE, RK_ST_WAIT_TIM
 RK_OK, RK_E_ARG, RK_E_CUDA, RK_E_UNSUPPORTED, RK_E_SIZE = 0, -1, -2, -3, -4
 RK_TW_N = 8192
 ABI_VERSION = 2
-RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL = -1, 0, 1, 2
+RK_PLACE_AUTO, RK_PLACE_GLOBAL, RK_PLACE_SMEM_STATE, RK_PLACE_SMEM_ALL, RK_PLACE_SMEM_U = -1, 0, 1, 2, 3
 
 # number of stage arrays and coefficient arrays per method (mirrors rk_evolve.cuh Traits)
 STAGE_ARRAYS = {RK_ETD35: 6, RK_ETD5: 6, RK_ETD34: 5, RK_ETD4: 4, RK_IF34: 5, RK_IF4: 4, RK_IF45DP: 7}

@@ -30,7 +30,7 @@ from .engine import DiagEnsemble
 # (threads per instance group, groups per block)
 SHAPES = ((32, 4), (32, 8), (32, 16), (64, 2), (64, 4), (64, 8), (128, 1), (128, 2), (128, 4), (256, 1),
           (256, 2))
-PLACES = (nat.RK_PLACE_SMEM_ALL, nat.RK_PLACE_SMEM_STATE, nat.RK_PLACE_GLOBAL)
+PLACES = (nat.RK_PLACE_SMEM_ALL, nat.RK_PLACE_SMEM_STATE, nat.RK_PLACE_SMEM_U, nat.RK_PLACE_GLOBAL)
 
 _CACHE: Dict[Tuple, Tuple[Tuple[int, int, int], ...]] = {}
 

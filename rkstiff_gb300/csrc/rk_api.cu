@@ -220,7 +220,7 @@ int validate_batch(const rk_batch* b, bool need_scratch) {
     set_error("rk_evolve: threads must be 0 (auto), 32, 64, 128 or 256");
     return RK_E_ARG;
   }
-  if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_ALL) {
+  if (b->placement < RK_PLACE_AUTO || b->placement > RK_PLACE_SMEM_U) {
     set_error("rk_evolve: unknown placement");
     return RK_E_ARG;
   }
@@ -410,7 +410,7 @@ int rk_evolve(const rk_batch* b, void* stream) {
     }
     int pl = b->class_place ? b->class_place[c] : b->placement;
     if (pl == RK_PLACE_AUTO) pl = auto_place(*b, n);
-    if (pl < RK_PLACE_GLOBAL || pl > RK_PLACE_SMEM_ALL) {
+    if (pl < RK_PLACE_GLOBAL || pl > RK_PLACE_SMEM_U) {
       set_error("rk_evolve: unknown class placement");
       return RK_E_ARG;
     }

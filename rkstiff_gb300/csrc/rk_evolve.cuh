@@ -1056,7 +1056,7 @@ RK_DEV bool ring_write(const rk_batch& b, int inst, const Group& g, const cx<T>*
 // the global slab), PL_SMEM_ALL (everything in shared memory; the coefficients are then
 // rebuilt at the start of every launch).
 // ---------------------------------------------------------------------------------
-enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2 };
+enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2, PL_SMEM_U = 3 };
 
 // Coefficient blocks of one instance (rk_batch.coef_blocks = nblk > 1), in its global slab:
 // block i at C0 + i * NC * mp, the blocks' h tags and the index of the block the next miss
@@ -1159,6 +1159,16 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.u = ssl;
   for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + ((U2 ? 1 : 2) + i) * x.mp : nullptr;
   x.unew = U2 ? x.N[1] : ssl + x.mp;
+  if constexpr (PLACE == PL_SMEM_U) {
+    // u and the new-state array (N2's for ETD35 / ETD5) in shared memory: u is read by every
+    // stage combination, and the two swap roles on every accepted step; the other stage
+    // arrays stay in the global slab (their slots of u and N2 there go unused)
+    cx<T>* sm = reinterpret_cast<cx<T>*>(sm_slab);
+    for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? gsl + ((U2 ? 1 : 2) + i) * x.mp : nullptr;
+    x.u = sm;
+    if (U2) x.N[1] = sm + x.mp;
+    x.unew = U2 ? x.N[1] : sm + x.mp;
+  }
   // global slab: [NV vectors | FP32 wavenumbers | coefficient block(s) | block tags]
   constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
   x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NV * x.mp)
@@ -1196,7 +1206,7 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     } else {
       // FP32: a working-precision copy after the coefficient block (shared memory when the
       // stage arrays are there, the global slab otherwise), filled once per launch
-      T* kw = PLACE == PL_GLOBAL ? reinterpret_cast<T*>(gsl + NV * x.mp)
+      T* kw = (PLACE == PL_GLOBAL || PLACE == PL_SMEM_U) ? reinterpret_cast<T*>(gsl + NV * x.mp)
             : PLACE == PL_SMEM_STATE ? reinterpret_cast<T*>(ssl + NV * x.mp)
                                      : reinterpret_cast<T*>(x.C + Tr::NC * x.mp);
       const double* kd = b.kx + mo;
@@ -1559,6 +1569,7 @@ template <class T, class CT, int METHOD>
 inline size_t smem_slab_bytes(int place, int64_t m) {
   const size_t mp = (size_t)round_up4(m);
   size_t bytes = 0;
+  if (place == PL_SMEM_U) return 2 * mp * sizeof(cx<T>);  // u and the new-state array
   if (place >= PL_SMEM_STATE) bytes += (size_t)traits_nv(METHOD) * mp * sizeof(cx<T>);
   if (place >= PL_SMEM_ALL) bytes += Traits<METHOD>::NC * mp * sizeof(CT);
   if (place >= PL_SMEM_STATE && sizeof(T) == sizeof(float)) bytes += mp * sizeof(T);  // wavenumbers

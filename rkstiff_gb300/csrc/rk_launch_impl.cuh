@@ -44,6 +44,10 @@ static int launch_evolve_p(const rk_batch& b, const ClassLaunch& c, cudaStream_t
     case RK_PLACE_GLOBAL: return launch_evolve_v<T, CT, S, M, LOGN, PL_GLOBAL>(b, c, st);
     case RK_PLACE_SMEM_STATE: return launch_evolve_v<T, CT, S, M, LOGN, PL_SMEM_STATE>(b, c, st);
     case RK_PLACE_SMEM_ALL: return launch_evolve_v<T, CT, S, M, LOGN, PL_SMEM_ALL>(b, c, st);
+    case RK_PLACE_SMEM_U:
+      set_error("placement RK_PLACE_SMEM_U is served by the compile-time ETD35 kernels (real operator, u*ux, "
+                "n = 256 .. 2048) only");
+      return RK_E_UNSUPPORTED;
   }
   set_error("unknown placement");
   return RK_E_ARG;

@@ -10,6 +10,7 @@ static int ct_2048(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
     case RK_PLACE_GLOBAL: return launch_evolve_v<T, T, double, RK_ETD35, 11, PL_GLOBAL>(b, c, s);
     case RK_PLACE_SMEM_STATE: return launch_evolve_v<T, T, double, RK_ETD35, 11, PL_SMEM_STATE>(b, c, s);
     case RK_PLACE_SMEM_ALL: return launch_evolve_v<T, T, double, RK_ETD35, 11, PL_SMEM_ALL>(b, c, s);
+    case RK_PLACE_SMEM_U: return launch_evolve_v<T, T, double, RK_ETD35, 11, PL_SMEM_U>(b, c, s);
   }
   return RK_E_UNSUPPORTED;
 }

@@ -102,7 +102,8 @@ def test_ensemble_placements_agree():
     a = run(128, nat.RK_PLACE_SMEM_STATE)
     b = run(128, nat.RK_PLACE_SMEM_ALL)
     assert np.array_equal(a, b)
-    for thr, place in ((64, nat.RK_PLACE_SMEM_STATE), (256, nat.RK_PLACE_SMEM_STATE), (128, nat.RK_PLACE_GLOBAL)):
+    for thr, place in ((64, nat.RK_PLACE_SMEM_STATE), (256, nat.RK_PLACE_SMEM_STATE), (128, nat.RK_PLACE_GLOBAL),
+                       (128, nat.RK_PLACE_SMEM_U), (64, nat.RK_PLACE_SMEM_U)):
         assert rel(run(thr, place), a) < 1e-5, (thr, place)
     eng.class_threads = None
     eng.class_place = None
