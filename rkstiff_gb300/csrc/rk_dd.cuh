@@ -356,7 +356,7 @@ RK_DEV float ser_comb(const float* __restrict__ tab, int row, const SerScale& s,
 // layouts C35_* (ETD35, ETD5) and C34_* (ETD34, ETD4); z in [-STIFF_Z, 80].  `tab`: a copy
 // of the method's table in shared memory (SH) or null (the global table)
 template <int METHOD, bool SH = false>
-RK_DEV void series_coeffs_f32(double zd, double hd, float* o, const float* tab = nullptr) {
+RK_DEV void series_coeffs_f32(double zd, double hd, float* o, const float* tab = nullptr, float* elo = nullptr) {
   const float zf = (float)zd, zl = (float)(zd - (double)zf), h = (float)hd;
   // The exponentials multiply u in every stage, so an error in them accumulates step after
   // step: they are formed in double-float and rounded once (one dd_exp of the smallest
@@ -374,6 +374,7 @@ RK_DEV void series_coeffs_f32(double zd, double hd, float* o, const float* tab =
     o[C35_E12] = e2.hi;
     o[C35_E34] = e3.hi;
     o[C35_E] = e4.hi;
+    if (elo) *elo = e4.lo;  // the low word of e^z, for the double-float state update
     o[C35_A21] = ser_comb<1, 0, 0, 4, SH>(T, 0, S14, h);
     o[C35_A31] = ser_comb<2, -1, 0, 8, SH>(T, 1, S14, h);
     o[C35_A32] = ser_comb<0, 1, 0, 8, SH>(T, 2, S14, h);

@@ -54,16 +54,41 @@ RK_HD int traits_nv(int method) { return traits_nn(method) + (unew_in_n2(method)
 // index of the block the next miss replaces
 constexpr int64_t RK_TAG_BYTES = 8 * (RK_COEF_BLOCKS_MAX + 4);
 
+// FP32 ETD35 / ETD5 with a real operator carry the state in double-float: two more complex
+// vectors after the stage vectors (the low FP32 words of u and of the new state) and one more
+// array in each coefficient block (the low word of E = e^z of the final combination).  The
+// stages and transforms stay FP32; only unew = E u + S is formed in double-float.
+RK_HD constexpr bool df_state(int method, int precision, int coef_complex) {
+  return precision == RK_FP32 && unew_in_n2(method) && !coef_complex;
+}
+// complex vectors and coefficient arrays (per block) of an instance's slab
+RK_HD int slab_nv(int method, int precision, int coef_complex) {
+  return traits_nv(method) + (df_state(method, precision, coef_complex) ? 2 : 0);
+}
+RK_HD int slab_nc(int method, int precision, int coef_complex) {
+  return num_coeffs(method) + (df_state(method, precision, coef_complex) ? 1 : 0);
+}
+
 RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m, int blocks = 1) {
   const int64_t mp = round_up4(m);
   const int64_t ts = precision == RK_FP64 ? 8 : 4;
   const int64_t vec = 2 * ts * mp;
   const int64_t coef = (coef_complex ? 2 : 1) * ts * mp;
   const int64_t kxw = precision == RK_FP64 ? 0 : ts * mp;
+  const int64_t nc = slab_nc(method, precision, coef_complex);
   // with several coefficient blocks: the extra blocks, then their h tags
-  const int64_t extra = blocks > 1 ? (blocks - 1) * num_coeffs(method) * coef + RK_TAG_BYTES : 0;
-  return traits_nv(method) * vec + num_coeffs(method) * coef + kxw + extra;
+  const int64_t extra = blocks > 1 ? (blocks - 1) * nc * coef + RK_TAG_BYTES : 0;
+  return slab_nv(method, precision, coef_complex) * vec + nc * coef + kxw + extra;
 }
+
+// the same counts at compile time for a kernel instantiation
+template <class T, class CT, int METHOD>
+struct SlabShape {
+  static constexpr bool DF = sizeof(T) == sizeof(float) && unew_in_n2(METHOD) && sizeof(CT) == sizeof(T);
+  static constexpr int NV = Traits<METHOD>::NN + (unew_in_n2(METHOD) ? 1 : 2);  // state vectors
+  static constexpr int NVS = NV + (DF ? 2 : 0);                                // with the low words
+  static constexpr int NCX = Traits<METHOD>::NC + (DF ? 1 : 0);                // arrays per block
+};
 
 // 2^(r/16), r = 0..15: the rungs of the learned controller's step-size ladder within an octave
 __constant__ const double k_ladder[16] = {
@@ -115,6 +140,8 @@ struct Ctx {
   const cx<T>* tws;  // compile-time path: the block's twiddle rows in shared memory
   CtlF cf;           // FP32 controller constants (FP32 working precision)
   const float* ser;  // the block's shared-memory copy of the FP32 series table, or null (global)
+  cx<T>* ulo;        // double-float state (df_state): low words of u and of the new state,
+  cx<T>* unlo;       // null otherwise; the low word of E = e^z is coefficient C35_N
   bool want_tail;    // the attempt's pass over unew also forms the tail-energy fraction
   mutable float tail_frac;  // that fraction (-1: not formed by the attempt)
   RK_DEV CT c(int idx, int j) const { return C[idx * mp + j]; }
@@ -470,7 +497,8 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
 template <class CT, class S, int METHOD, bool FAST>
 __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const cx<double>* __restrict__ lin,
                                                  CT* __restrict__ C, double h, EtdCfg ec,
-                                                 const float* __restrict__ ser = nullptr) {
+                                                 const float* __restrict__ ser = nullptr,
+                                                 float* __restrict__ elo = nullptr) {
   constexpr int NC = Traits<METHOD>::NC;
   if (!is_etd(METHOD)) {
     for (int j = g.tid; j < m; j += g.nthr) {
@@ -498,8 +526,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
           // each combination's own Taylor series in FP32 (series_coeffs_f32): the FP64
           // series would hold the whole warp on the 1/64-rate FP64 pipe for one small mode
           float of[NC];
-          if (ser) series_coeffs_f32<METHOD, true>(sre(z), h, of, ser);
-          else series_coeffs_f32<METHOD>(sre(z), h, of);
+          if (ser) series_coeffs_f32<METHOD, true>(sre(z), h, of, ser, elo ? elo + j : nullptr);
+          else series_coeffs_f32<METHOD>(sre(z), h, of, nullptr, elo ? elo + j : nullptr);
 #pragma unroll
           for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         } else {
@@ -518,6 +546,7 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
         // stiff: FP32 arithmetic in a form without cancellation (a few FP32 ulps)
         float of[NC];
         stiff_coeffs_f32<METHOD>(zr, h, of);
+        if (elo) elo[j] = 0.f;  // e^z < e^-32: its low word is below every other term
 #pragma unroll
         for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         continue;
@@ -525,8 +554,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
       if (zr <= 80.0) {
         // FP32 series / stiff forms per combination (series_coeffs_f32)
         float of[NC];
-        if (ser) series_coeffs_f32<METHOD, true>(zr, h, of, ser);
-        else series_coeffs_f32<METHOD>(zr, h, of);
+        if (ser) series_coeffs_f32<METHOD, true>(zr, h, of, ser, elo ? elo + j : nullptr);
+        else series_coeffs_f32<METHOD>(zr, h, of, nullptr, elo ? elo + j : nullptr);
 #pragma unroll
         for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         continue;
@@ -534,6 +563,12 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
       double E[4];
       fast_real_psi(METHOD, zr, h, E, reinterpret_cast<double*>(P));
       etd_from_psi_e<double>(METHOD, E, reinterpret_cast<double*>(P), reinterpret_cast<double*>(o));
+      if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) {
+        if (elo) {
+          const double e = reinterpret_cast<double*>(o)[C35_E];
+          elo[j] = (float)(e - (double)(float)e);
+        }
+      }
     } else if constexpr (FAST && sizeof(S) == sizeof(double)) {
       double E[4];
       fast_real_psi(METHOD, sre(z), h, E, reinterpret_cast<double*>(P));
@@ -596,7 +631,9 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
 
 template <class T, class CT, class S, int METHOD, int LOGN>
 RK_DEV void compute_coeffs(const Ctx<T, CT, LOGN>& x, double h, const EtdCfg& ec) {
-  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, x.ser);
+  float* elo = nullptr;
+  if constexpr (SlabShape<T, CT, METHOD>::DF) elo = reinterpret_cast<float*>(x.C + Traits<METHOD>::NC * x.mp);
+  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, x.ser, elo);
 }
 
 // ---------------------------------------------------------------------------------
@@ -815,9 +852,46 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
     return ((((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A71, j), N[0][j])) + cmul(x.c(C35_A73, j), N[2][j])) +
              cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) + cmul(x.c(C35_A76, j), N[5][j]);
   };
+  // Double-float state (x.ulo set: FP32, real operator): unew = E u + S with u = u_hi +
+  // u_lo and E = E_hi + E_lo, S the FP32 sum of the a7k N_k terms; E_hi u_hi exactly as a
+  // product and its rounding error (FMA), the cross terms and the rounding of the sum with S
+  // (TwoSum) collected in the low word.  Returns the high word; the low word goes to unlo.
+  // Rounding u to FP32 on every accepted step, and E to FP32, is what accumulates over a
+  // long run; the stage values' FP32 error enters only through h-scaled terms.
+  auto k7df = [&](int j) {
+    if constexpr (sizeof(T) == sizeof(float) && sizeof(CT) == sizeof(T)) {
+      const cx<T> S = (((cmul(x.c(C35_A71, j), N[0][j]) + cmul(x.c(C35_A73, j), N[2][j])) +
+                        cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) +
+                      cmul(x.c(C35_A76, j), N[5][j]);
+      const float eh = x.c(C35_E, j), el = x.c(C35_N, j);
+      const cx<T> uh = u[j], ul = x.ulo[j];
+      auto part = [&](float h, float l, float sv, float& lo_out) {
+        const float p = eh * h;
+        const float ep = fmaf(eh, h, -p);  // exact: E_hi u_hi = p + ep
+        const float corr = fmaf(eh, l, fmaf(el, h, ep));
+        const float q = p + sv;  // TwoSum(p, sv)
+        const float bb = q - p;
+        const float e2 = (p - (q - bb)) + (sv - bb);
+        const float lo = e2 + corr;
+        const float hi = q + lo;
+        lo_out = lo - (hi - q);
+        return hi;
+      };
+      cx<T> lo;
+      const cx<T> hi{part(uh.x, ul.x, S.x, lo.x), part(uh.y, ul.y, S.y, lo.y)};
+      x.unlo[j] = lo;
+      return hi;
+    } else {
+      return k7(j);
+    }
+  };
   if (!adaptive) {
     // ETD5: unew, then N1 <- N(unew) (FSAL, etd5.py:260)
-    for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7(j);
+    if (x.ulo) {
+      for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7df(j);
+    } else {
+      for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7(j);
+    }
     x.g.sync();
     const cx<T>* un = x.unew;
     nl_eval(x, [&](int j) { return un[j]; }, N[0]);
@@ -829,6 +903,7 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
     return cmul(x.c(C35_A75, j), s);
   };
   if constexpr (sizeof(T) == sizeof(float)) {
+    if (x.ulo) return unew_and_s_f32(x, k7df, err, x.cf, 4);
     return unew_and_s_f32(x, k7, err, x.cf, 4);
   } else {
     double mx = write_unew(x, k7);
@@ -1069,10 +1144,10 @@ enum { PL_GLOBAL = 0, PL_SMEM_STATE = 1, PL_SMEM_ALL = 2, PL_SMEM_U = 3 };
 // come from local memory instead of registers or the parameter bank.
 template <class T, class CT, int METHOD>
 RK_DEV CT* coef_block0(unsigned char* slab, int mp) {
-  constexpr int NV = Traits<METHOD>::NN + (unew_in_n2(METHOD) ? 1 : 2);
+  constexpr int NVS = SlabShape<T, CT, METHOD>::NVS;
   constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
   cx<T>* gsl = reinterpret_cast<cx<T>*>(slab);
-  return reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NV * mp) + KXW * mp);
+  return reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NVS * mp) + KXW * mp);
 }
 template <class T, class CT, int METHOD>
 RK_DEV double* coef_tags(unsigned char* slab, int m, int nblk) {
@@ -1094,7 +1169,7 @@ template <class T, class CT, int METHOD>
 __device__ __noinline__ CoefPick<CT> coef_block(unsigned char* slab, Group g, int mp, int m, int nblk, double h) {
   double* tags = coef_tags<T, CT, METHOD>(slab, m, nblk);
   CT* const C0 = coef_block0<T, CT, METHOD>(slab, mp);
-  const int64_t blk = (int64_t)Traits<METHOD>::NC * mp;
+  const int64_t blk = (int64_t)SlabShape<T, CT, METHOD>::NCX * mp;
   int hit = -1;
   for (int i = 0; i < nblk; ++i)
     if (tags[i] == h) hit = i;
@@ -1126,7 +1201,7 @@ __device__ __noinline__ CoefPick<CT> coef_block_resume(unsigned char* slab, Grou
   for (int i = 0; i < nblk; ++i)
     if (tags[i] == hc) found = i;
   if (found < 0) return CoefPick<CT>{C, __longlong_as_double(0x7ff8000000000000ULL)};  // rebuild first
-  return CoefPick<CT>{coef_block0<T, CT, METHOD>(slab, mp) + found * (int64_t)Traits<METHOD>::NC * mp, hc};
+  return CoefPick<CT>{coef_block0<T, CT, METHOD>(slab, mp) + found * (int64_t)SlabShape<T, CT, METHOD>::NCX * mp, hc};
 }
 
 // u <- unew after an accepted step.  With the new state in N2's array the two arrays swap
@@ -1135,6 +1210,7 @@ template <bool U2, class X>
 RK_DEV void accept_swap(X& x) {
   cx_ptr_swap(x.u, U2 ? x.N[1] : x.unew);
   if (U2) x.unew = x.N[1];
+  if (x.ulo) cx_ptr_swap(x.ulo, x.unlo);
 }
 
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
@@ -1155,10 +1231,18 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   cx<T>* gsl = reinterpret_cast<cx<T>*>(reinterpret_cast<char*>(b.slab) + b.slab_off[inst]);
   cx<T>* ssl = PLACE == PL_GLOBAL ? gsl : reinterpret_cast<cx<T>*>(sm_slab);
   constexpr bool U2 = unew_in_n2(METHOD);
-  constexpr int NV = Tr::NN + (U2 ? 1 : 2);  // complex vectors before the coefficient block
+  using SS = SlabShape<T, CT, METHOD>;
+  constexpr int NV = SS::NV;    // state vectors u, (unew,) N1..NN
+  constexpr int NVS = SS::NVS;  // and, with the double-float state, the low words of u and unew
   x.u = ssl;
   for (int i = 0; i < 8; ++i) x.N[i] = (i < Tr::NN) ? ssl + ((U2 ? 1 : 2) + i) * x.mp : nullptr;
   x.unew = U2 ? x.N[1] : ssl + x.mp;
+  // the low words of u and unew: in shared memory with everything else under PL_SMEM_ALL
+  // (small grids, where shared memory has room), in the global slab otherwise (they cost a
+  // resident block of the larger grids' shared-memory placements)
+  cx<T>* lsl = PLACE == PL_SMEM_ALL ? ssl : gsl;
+  x.ulo = SS::DF ? lsl + NV * x.mp : nullptr;
+  x.unlo = SS::DF ? lsl + (NV + 1) * x.mp : nullptr;
   if constexpr (PLACE == PL_SMEM_U) {
     // u and the new-state array (N2's for ETD35 / ETD5) in shared memory: u is read by every
     // stage combination, and the two swap roles on every accepted step; the other stage
@@ -1169,10 +1253,10 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     if (U2) x.N[1] = sm + x.mp;
     x.unew = U2 ? x.N[1] : sm + x.mp;
   }
-  // global slab: [NV vectors | FP32 wavenumbers | coefficient block(s) | block tags]
+  // global slab: [NVS vectors | FP32 wavenumbers | coefficient block(s) of NCX arrays | tags]
   constexpr int KXW = sizeof(T) == sizeof(float) ? 1 : 0;
-  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NV * x.mp)
-                             : reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NV * x.mp) + KXW * x.mp);
+  x.C = PLACE == PL_SMEM_ALL ? reinterpret_cast<CT*>(ssl + NVS * x.mp)
+                             : reinterpret_cast<CT*>(reinterpret_cast<T*>(gsl + NVS * x.mp) + KXW * x.mp);
   x.fa = fa;
   x.fb = fb;
   x.red = red;
@@ -1206,9 +1290,9 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
     } else {
       // FP32: a working-precision copy after the coefficient block (shared memory when the
       // stage arrays are there, the global slab otherwise), filled once per launch
-      T* kw = (PLACE == PL_GLOBAL || PLACE == PL_SMEM_U) ? reinterpret_cast<T*>(gsl + NV * x.mp)
+      T* kw = (PLACE == PL_GLOBAL || PLACE == PL_SMEM_U) ? reinterpret_cast<T*>(gsl + NVS * x.mp)
             : PLACE == PL_SMEM_STATE ? reinterpret_cast<T*>(ssl + NV * x.mp)
-                                     : reinterpret_cast<T*>(x.C + Tr::NC * x.mp);
+                                     : reinterpret_cast<T*>(x.C + SS::NCX * x.mp);
       const double* kd = b.kx + mo;
       for (int j = g.tid; j < x.m; j += g.nthr) kw[j] = T(kd[j]);
       x.kx = kw;
@@ -1216,6 +1300,18 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   }
   cx<T>* uio = reinterpret_cast<cx<T>*>(b.u) + mo;
   for (int j = g.tid; j < x.m; j += g.nthr) x.u[j] = uio[j];
+  // Double-float state: u's low words continue from the previous launch of this evolve (it
+  // saved them in the slab's first low-word array and set reserved_i), else start at zero (a
+  // fresh state, a step() call, a noalloc call); E's low words come with the coefficients.
+  if (x.ulo) {
+    cx<T>* lo0 = gsl + NV * x.mp;
+    const bool keep = b.run_mode == RK_RUN_EVOLVE && st.reserved_i == 1;
+    if (!keep) {
+      for (int j = g.tid; j < x.m; j += g.nthr) x.ulo[j] = cx<T>{T(0), T(0)};
+    } else if (x.ulo != lo0) {
+      for (int j = g.tid; j < x.m; j += g.nthr) x.ulo[j] = lo0[j];
+    }
+  }
   g.sync();
 
   double t = st.t, tf = st.tf, h = st.h;
@@ -1402,7 +1498,14 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   }
   g.sync();
   for (int j = g.tid; j < x.m; j += g.nthr) uio[j] = x.u[j];
+  if (x.ulo) {
+    // the low words of the final state, where the next launch of this evolve looks for them
+    cx<T>* lo0 = gsl + NV * x.mp;
+    if (x.ulo != lo0)
+      for (int j = g.tid; j < x.m; j += g.nthr) lo0[j] = x.ulo[j];
+  }
   if (g.tid == 0) {
+    if (x.ulo) st.reserved_i = 1;
     st.t = t;
     st.h = h;
     st.h_coeff = PLACE == PL_SMEM_ALL ? nan_d() : hc;
@@ -1569,9 +1672,11 @@ template <class T, class CT, int METHOD>
 inline size_t smem_slab_bytes(int place, int64_t m) {
   const size_t mp = (size_t)round_up4(m);
   size_t bytes = 0;
+  using SS = SlabShape<T, CT, METHOD>;
   if (place == PL_SMEM_U) return 2 * mp * sizeof(cx<T>);  // u and the new-state array
-  if (place >= PL_SMEM_STATE) bytes += (size_t)traits_nv(METHOD) * mp * sizeof(cx<T>);
-  if (place >= PL_SMEM_ALL) bytes += Traits<METHOD>::NC * mp * sizeof(CT);
+  // the state vectors; under PL_SMEM_ALL with the double-float state's low words
+  if (place >= PL_SMEM_STATE) bytes += (size_t)(place == PL_SMEM_ALL ? SS::NVS : SS::NV) * mp * sizeof(cx<T>);
+  if (place >= PL_SMEM_ALL) bytes += SS::NCX * mp * sizeof(CT);
   if (place >= PL_SMEM_STATE && sizeof(T) == sizeof(float)) bytes += mp * sizeof(T);  // wavenumbers
   return bytes;
 }

@@ -51,12 +51,14 @@ static ctx_get_current_fn ctx_get_current() {
 
 // Offsets of instance i's slab: a uniform stride (the slab of the largest grid), so no
 // per-instance sizes are read back from the device.  Also invalidates each instance's
-// cached coefficients: the shared array holds whatever the previous call left there.
+// cached coefficients and saved low state words: the shared array holds whatever the
+// previous call left there.
 __global__ void noalloc_prepare_kernel(int64_t* slab_off, int64_t n_inst, int64_t stride, rk_inst_state* state) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_inst) return;
   slab_off[i] = i * stride;
   state[i].h_coeff = __longlong_as_double(0x7ff8000000000000ULL);
+  state[i].reserved_i = 0;  // nor are the low words of a double-float state kept there
 }
 
 }  // namespace rk

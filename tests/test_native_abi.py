@@ -42,8 +42,13 @@ def test_abi_version_and_sizes(lib):
     assert lib.rk_num_coeffs(nat.RK_IF34) == 2
     assert lib.rk_num_coeffs(nat.RK_IF45DP) == 28
     assert lib.rk_num_coeffs(99) < 0
-    # ETD35, FP32, real coefficients, m=513 -> mp=516: 7 complex arrays (the new state shares N2's) + 21 real arrays + wavenumbers
-    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 0, 513) == 7 * 8 * 516 + 21 * 4 * 516 + 4 * 516
+    # ETD35, FP32, real coefficients, m=513 -> mp=516: 7 complex arrays (the new state shares N2's) and the
+    # double-float state's low words of u and of the new state (2 complex arrays), 21 real coefficient arrays
+    # and the low word of e^z, the FP32 wavenumbers
+    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 0, 513) == 9 * 8 * 516 + 22 * 4 * 516 + 4 * 516
+    # two coefficient blocks of 22 arrays, then their tags (RK_COEF_BLOCKS_MAX = 4 doubles + 4)
+    assert lib.rk_slab_bytes_blocks(nat.RK_ETD35, nat.RK_FP32, 0, 513, 2) == \
+        9 * 8 * 516 + 2 * 22 * 4 * 516 + 4 * 516 + 8 * (4 + 4)
     assert lib.rk_slab_bytes(nat.RK_IF34, nat.RK_FP64, 1, 100) == 7 * 16 * 100 + 2 * 16 * 100
     assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP64, 0, 0) < 0
 
