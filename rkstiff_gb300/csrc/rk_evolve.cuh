@@ -7,6 +7,8 @@
 // accept/reject rule (solveras.py:384-410, 457-554).
 #pragma once
 
+#include <type_traits>
+
 #include "rk_coeffs.cuh"
 #include "rk_dd.cuh"
 #include "rk_common.cuh"
@@ -758,6 +760,12 @@ RK_DEV double controller_s(const Ctx<T, CT, LOGN>& x, double maxu, EF ef, const 
   }
 }
 
+// the new state of one mode as a double-float pair (high and low FP32 words)
+template <class T>
+struct HiLo {
+  cx<T> hi, lo;
+};
+
 // ETD35 in FP32 working precision: unew and |err|^2 in one pass over the modes (the error
 // combination reads the same stage vectors as unew), |unew|^2 and |err|^2 of each mode
 // parked in the FFT buffer (free between attempts) until the group maximum of |unew|^2 is
@@ -770,8 +778,17 @@ RK_DEV double unew_and_s_f32(const Ctx<T, CT, LOGN>& x, KF kf, EF ef, const CtlF
   float mx = 0.f;
   bool nan = false;
   auto one = [&](int j) {
-    const cx<T> v = kf(j);
+    const auto r = kf(j);
     const cx<T> e = ef(j);
+    // stores after both combinations have read the stage vectors (a store before them could
+    // alias those arrays as far as the compiler knows, and make it load them again)
+    cx<T> v;
+    if constexpr (std::is_same<typename std::decay<decltype(r)>::type, HiLo<T>>::value) {
+      v = r.hi;
+      x.unlo[j] = r.lo;
+    } else {
+      v = r;
+    }
     x.unew[j] = v;
     const float a2 = v.x * v.x + v.y * v.y;
     if (a2 != a2) nan = true;
@@ -855,7 +872,7 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
   // Double-float state (x.ulo set: FP32, real operator): unew = E u + S with u = u_hi +
   // u_lo and E = E_hi + E_lo, S the FP32 sum of the a7k N_k terms; E_hi u_hi exactly as a
   // product and its rounding error (FMA), the cross terms and the rounding of the sum with S
-  // (TwoSum) collected in the low word.  Returns the high word; the low word goes to unlo.
+  // (TwoSum) collected in the low word.  Returns both words (the caller stores them).
   // Rounding u to FP32 on every accepted step, and E to FP32, is what accumulates over a
   // long run; the stage values' FP32 error enters only through h-scaled terms.
   auto k7df = [&](int j) {
@@ -877,18 +894,21 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
         lo_out = lo - (hi - q);
         return hi;
       };
-      cx<T> lo;
-      const cx<T> hi{part(uh.x, ul.x, S.x, lo.x), part(uh.y, ul.y, S.y, lo.y)};
-      x.unlo[j] = lo;
-      return hi;
+      HiLo<T> r;
+      r.hi = cx<T>{part(uh.x, ul.x, S.x, r.lo.x), part(uh.y, ul.y, S.y, r.lo.y)};
+      return r;
     } else {
-      return k7(j);
+      return HiLo<T>{k7(j), cx<T>{T(0), T(0)}};
     }
   };
   if (!adaptive) {
     // ETD5: unew, then N1 <- N(unew) (FSAL, etd5.py:260)
     if (x.ulo) {
-      for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7df(j);
+      for (int j = x.g.tid; j < x.m; j += x.g.nthr) {
+        const HiLo<T> r = k7df(j);
+        x.unew[j] = r.hi;
+        x.unlo[j] = r.lo;
+      }
     } else {
       for (int j = x.g.tid; j < x.m; j += x.g.nthr) x.unew[j] = k7(j);
     }
