@@ -111,7 +111,7 @@ typedef struct rk_inst_state {
   int32_t accept;    /* last attempt accepted (reference _accept)                  */
   int32_t snap_count;/* snapshots written in the current launch                     */
   int32_t reserved_i;/* diagonal kernels: 1 once a launch saved the low words of a double-float
-                        state (FP32 ETD35 / ETD5, real operator); a fresh state has 0 */
+                        state (FP32 ETD35 / ETD5); a fresh state has 0 */
   int64_t steps, attempts, rejects, nl_evals, coeff_updates, reserved_l;
 } rk_inst_state;
 
@@ -258,8 +258,8 @@ int rk_fill_twiddles(void* tw64, void* tw32, void* stream);
 
 /* Bytes of per-instance scratch rk_evolve needs for an instance with m modes.
  * Replaces the coefficient / stage arrays the reference allocates per solver object
- * (e.g. rkstiff/etd35.py:129-155).  FP32 ETD35 / ETD5 with real coefficients and one
- * coefficient block also hold the low FP32 words of a double-float state and of e^z. */
+ * (e.g. rkstiff/etd35.py:129-155).  FP32 ETD35 / ETD5 also hold the low FP32 words of a
+ * double-float state (u and the new state) and of e^z (one more array per coefficient block). */
 int64_t rk_slab_bytes(int32_t method, int32_t precision, int32_t coef_complex, int64_t m);
 /* The same with `blocks` coefficient blocks (rk_batch.coef_blocks, 1..RK_COEF_BLOCKS_MAX). */
 int64_t rk_slab_bytes_blocks(int32_t method, int32_t precision, int32_t coef_complex, int64_t m, int32_t blocks);

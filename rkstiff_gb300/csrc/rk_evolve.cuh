@@ -56,12 +56,12 @@ RK_HD int traits_nv(int method) { return traits_nn(method) + (unew_in_n2(method)
 // index of the block the next miss replaces
 constexpr int64_t RK_TAG_BYTES = 8 * (RK_COEF_BLOCKS_MAX + 4);
 
-// FP32 ETD35 / ETD5 with a real operator carry the state in double-float: two more complex
+// FP32 ETD35 / ETD5 carry the state in double-float: two more complex
 // vectors after the stage vectors (the low FP32 words of u and of the new state) and one more
 // array in each coefficient block (the low word of E = e^z of the final combination).  The
 // stages and transforms stay FP32; only unew = E u + S is formed in double-float.
 RK_HD constexpr bool df_state(int method, int precision, int coef_complex) {
-  return precision == RK_FP32 && unew_in_n2(method) && !coef_complex;
+  return precision == RK_FP32 && unew_in_n2(method) && coef_complex >= 0;
 }
 // complex vectors and coefficient arrays (per block) of an instance's slab
 RK_HD int slab_nv(int method, int precision, int coef_complex) {
@@ -86,7 +86,7 @@ RK_HD int64_t slab_bytes(int method, int precision, int coef_complex, int64_t m,
 // the same counts at compile time for a kernel instantiation
 template <class T, class CT, int METHOD>
 struct SlabShape {
-  static constexpr bool DF = sizeof(T) == sizeof(float) && unew_in_n2(METHOD) && sizeof(CT) == sizeof(T);
+  static constexpr bool DF = sizeof(T) == sizeof(float) && unew_in_n2(METHOD);
   static constexpr int NV = Traits<METHOD>::NN + (unew_in_n2(METHOD) ? 1 : 2);  // state vectors
   static constexpr int NVS = NV + (DF ? 2 : 0);                                // with the low words
   static constexpr int NCX = Traits<METHOD>::NC + (DF ? 1 : 0);                // arrays per block
@@ -483,6 +483,12 @@ if constexpr (uux_fused(LOGN)) {
 // ---------------------------------------------------------------------------------
 template <class T> RK_DEV void store_c(T& d, double v) { d = T(v); }
 template <class T> RK_DEV void store_c(cx<T>& d, cx<double> v) { d = cx<T>{T(v.x), T(v.y)}; }
+// the low word of v after store_c (the double-float state's E_lo)
+RK_DEV void store_lo(float& d, double v) { d = (float)(v - (double)(float)v); }
+RK_DEV void store_lo(cx<float>& d, cx<double> v) {
+  d = cx<float>{(float)(v.x - (double)(float)v.x), (float)(v.y - (double)(float)v.y)};
+}
+template <class T, class V> RK_DEV void store_lo(T&, V) {}
 
 template <class S> RK_DEV S load_z(const cx<double>* lin, int j, double h);
 template <> RK_DEV double load_z<double>(const cx<double>* lin, int j, double h) { return h * lin[j].x; }
@@ -500,7 +506,7 @@ template <class CT, class S, int METHOD, bool FAST>
 __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const cx<double>* __restrict__ lin,
                                                  CT* __restrict__ C, double h, EtdCfg ec,
                                                  const float* __restrict__ ser = nullptr,
-                                                 float* __restrict__ elo = nullptr) {
+                                                 CT* __restrict__ elo = nullptr) {
   constexpr int NC = Traits<METHOD>::NC;
   if (!is_etd(METHOD)) {
     for (int j = g.tid; j < m; j += g.nthr) {
@@ -538,6 +544,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
           etd_from_psi_e<S>(METHOD, E, P, o);
 #pragma unroll
           for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+          if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5)
+            if (elo) store_lo(elo[j], o[C35_E]);
         }
         continue;
       }
@@ -587,6 +595,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
     }
 #pragma unroll
     for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+    if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5)
+      if (elo) store_lo(elo[j], o[C35_E]);
   }
   if constexpr (FAST) {
     g.sync();
@@ -633,8 +643,8 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
 
 template <class T, class CT, class S, int METHOD, int LOGN>
 RK_DEV void compute_coeffs(const Ctx<T, CT, LOGN>& x, double h, const EtdCfg& ec) {
-  float* elo = nullptr;
-  if constexpr (SlabShape<T, CT, METHOD>::DF) elo = reinterpret_cast<float*>(x.C + Traits<METHOD>::NC * x.mp);
+  CT* elo = nullptr;
+  if constexpr (SlabShape<T, CT, METHOD>::DF) elo = x.C + Traits<METHOD>::NC * x.mp;
   compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, x.ser, elo);
 }
 
@@ -869,7 +879,7 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
     return ((((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A71, j), N[0][j])) + cmul(x.c(C35_A73, j), N[2][j])) +
              cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) + cmul(x.c(C35_A76, j), N[5][j]);
   };
-  // Double-float state (x.ulo set: FP32, real operator): unew = E u + S with u = u_hi +
+  // Double-float state (x.ulo set: FP32): unew = E u + S with u = u_hi +
   // u_lo and E = E_hi + E_lo, S the FP32 sum of the a7k N_k terms; E_hi u_hi exactly as a
   // product and its rounding error (FMA), the cross terms and the rounding of the sum with S
   // (TwoSum) collected in the low word.  Returns both words (the caller stores them).
@@ -896,6 +906,30 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
       };
       HiLo<T> r;
       r.hi = cx<T>{part(uh.x, ul.x, S.x, r.lo.x), part(uh.y, ul.y, S.y, r.lo.y)};
+      return r;
+    } else if constexpr (sizeof(T) == sizeof(float)) {
+      // complex E (an operator with imaginary parts, e.g. the NLS dispersion): each component
+      // of E_hi u_hi is a sum of two products, both taken exactly
+      const cx<T> S = (((cmul(x.c(C35_A71, j), N[0][j]) + cmul(x.c(C35_A73, j), N[2][j])) +
+                        cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) +
+                      cmul(x.c(C35_A76, j), N[5][j]);
+      const cx<T> eh = x.c(C35_E, j), el = x.c(C35_N, j);
+      const cx<T> uh = u[j], ul = x.ulo[j];
+      // a1 b1 + a2 b2 + la + sv: the two products and the sums' rounding in the low word
+      auto comp = [&](float a1, float b1, float a2, float b2, float la, float sv, float& lo_out) {
+        const float p1 = a1 * b1, e1 = fmaf(a1, b1, -p1);
+        const float p2 = a2 * b2, e2 = fmaf(a2, b2, -p2);
+        const float q = p1 + p2, qb = q - p1, e3 = (p1 - (q - qb)) + (p2 - qb);
+        const float r = q + sv, rb = r - q, e4 = (q - (r - rb)) + (sv - rb);
+        const float lo = ((e1 + e2) + (e3 + e4)) + la;
+        const float hi = r + lo;
+        lo_out = lo - (hi - r);
+        return hi;
+      };
+      const float la_re = fmaf(eh.x, ul.x, -eh.y * ul.y) + fmaf(el.x, uh.x, -el.y * uh.y);
+      const float la_im = fmaf(eh.x, ul.y, eh.y * ul.x) + fmaf(el.x, uh.y, el.y * uh.x);
+      HiLo<T> r;
+      r.hi = cx<T>{comp(eh.x, uh.x, -eh.y, uh.y, la_re, S.x, r.lo.x), comp(eh.x, uh.y, eh.y, uh.x, la_im, S.y, r.lo.y)};
       return r;
     } else {
       return HiLo<T>{k7(j), cx<T>{T(0), T(0)}};

@@ -50,6 +50,8 @@ def test_abi_version_and_sizes(lib):
     assert lib.rk_slab_bytes_blocks(nat.RK_ETD35, nat.RK_FP32, 0, 513, 2) == \
         9 * 8 * 516 + 2 * 22 * 4 * 516 + 4 * 516 + 8 * (4 + 4)
     assert lib.rk_slab_bytes(nat.RK_IF34, nat.RK_FP64, 1, 100) == 7 * 16 * 100 + 2 * 16 * 100
+    # ETD35 FP32 with complex coefficients: the low word of e^z is a complex array
+    assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP32, 1, 100) == 9 * 8 * 100 + 22 * 8 * 100 + 4 * 100
     assert lib.rk_slab_bytes(nat.RK_ETD35, nat.RK_FP64, 0, 0) < 0
 
 
