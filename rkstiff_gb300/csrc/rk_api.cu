@@ -103,7 +103,7 @@ static size_t max_smem_per_block() {
 // calls); an evolve may rebuild them in shared memory once per launch.
 static int auto_place(const rk_batch& b, int n) {
   const size_t tw = (size_t)fpad_size(n) * (b.precision == RK_FP64 ? 16 : 8) +  // compile-time kernels' table
-                    (b.mlp != nullptr ? ((RK_MLP_PACK_BYTES + 15) & ~15) + 17 * RK_SER_NC * RK_SER_NT * 4 : 0);
+                    (b.mlp != nullptr ? ((RK_MLP_PACK_BYTES + 15) & ~15) : 0);
   const size_t lim1 = max_smem_per_block();
   const size_t lim2 = lim1 / 2 - 1024;
   const bool step = b.run_mode == RK_RUN_STEP;
@@ -127,9 +127,8 @@ static int auto_groups(int threads) { return threads >= 128 ? 1 : 128 / threads;
 static int launch_class(const rk_batch& b, const ClassLaunch& c, cudaStream_t s) {
   const int nn = c.n > 0 ? c.n : b.n_max;
   const size_t tw_bytes = (size_t)fpad_size(nn) * (b.precision == RK_FP64 ? 16 : 8);  // compile-time kernels' table
-  // learned-controller launches add block-wide copies of the inference buffer and the
-  // FP32 coefficient series table (at most the ETD35 one)
-  const size_t learned = b.mlp != nullptr ? ((RK_MLP_PACK_BYTES + 15) & ~15) + 17 * RK_SER_NC * RK_SER_NT * 4 : 0;
+  // learned-controller launches add a block-wide copy of the inference buffer
+  const size_t learned = b.mlp != nullptr ? ((RK_MLP_PACK_BYTES + 15) & ~15) : 0;
   if (smem_bytes_method(b, nn, c.place) * (size_t)c.groups + tw_bytes + learned > max_smem_per_block()) {
     set_error("rk_evolve: placement " + std::to_string(c.place) + " needs more shared memory than a block has");
     return RK_E_SIZE;

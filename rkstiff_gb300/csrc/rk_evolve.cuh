@@ -141,7 +141,6 @@ struct Ctx {
   const cx<T>* tw;   // global table of RK_TW_N twiddles
   const cx<T>* tws;  // compile-time path: the block's twiddle rows in shared memory
   CtlF cf;           // FP32 controller constants (FP32 working precision)
-  const float* ser;  // the block's shared-memory copy of the FP32 series table, or null (global)
   cx<T>* ulo;        // double-float state (df_state): low words of u and of the new state,
   cx<T>* unlo;       // null otherwise; the low word of E = e^z is coefficient C35_N
   bool want_tail;    // the attempt's pass over unew also forms the tail-energy fraction
@@ -505,7 +504,6 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
 template <class CT, class S, int METHOD, bool FAST>
 __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const cx<double>* __restrict__ lin,
                                                  CT* __restrict__ C, double h, EtdCfg ec,
-                                                 const float* __restrict__ ser = nullptr,
                                                  CT* __restrict__ elo = nullptr) {
   constexpr int NC = Traits<METHOD>::NC;
   if (!is_etd(METHOD)) {
@@ -534,8 +532,7 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
           // each combination's own Taylor series in FP32 (series_coeffs_f32): the FP64
           // series would hold the whole warp on the 1/64-rate FP64 pipe for one small mode
           float of[NC];
-          if (ser) series_coeffs_f32<METHOD, true>(sre(z), h, of, ser, elo ? elo + j : nullptr);
-          else series_coeffs_f32<METHOD>(sre(z), h, of, nullptr, elo ? elo + j : nullptr);
+          series_coeffs_f32<METHOD>(sre(z), h, of, nullptr, elo ? elo + j : nullptr);
 #pragma unroll
           for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         } else {
@@ -564,8 +561,7 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
       if (zr <= 80.0) {
         // FP32 series / stiff forms per combination (series_coeffs_f32)
         float of[NC];
-        if (ser) series_coeffs_f32<METHOD, true>(zr, h, of, ser, elo ? elo + j : nullptr);
-        else series_coeffs_f32<METHOD>(zr, h, of, nullptr, elo ? elo + j : nullptr);
+        series_coeffs_f32<METHOD>(zr, h, of, nullptr, elo ? elo + j : nullptr);
 #pragma unroll
         for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
         continue;
@@ -645,7 +641,7 @@ template <class T, class CT, class S, int METHOD, int LOGN>
 RK_DEV void compute_coeffs(const Ctx<T, CT, LOGN>& x, double h, const EtdCfg& ec) {
   CT* elo = nullptr;
   if constexpr (SlabShape<T, CT, METHOD>::DF) elo = x.C + Traits<METHOD>::NC * x.mp;
-  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, x.ser, elo);
+  compute_coeffs_impl<CT, S, METHOD, sizeof(T) == sizeof(float)>(x.g, x.m, x.mp, x.lin, x.C, h, ec, elo);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1270,7 +1266,7 @@ RK_DEV void accept_swap(X& x) {
 template <class T, class CT, class S, int METHOD, int LOGN, int PLACE>
 RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa, cx<T>* fb, double* red,
                          unsigned char* sm_slab, const cx<T>* tws, float* mlp_s, int nfft,
-                         const unsigned char* mlpw, const float* ser) {
+                         const unsigned char* mlpw) {
   using Tr = Traits<METHOD>;
   Ctx<T, CT, LOGN> x;
   x.g = g;
@@ -1317,7 +1313,6 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
   x.tw = reinterpret_cast<const cx<T>*>(b.twiddle);
   x.tws = tws;
   x.cf = make_ctlf(b.ctl);
-  x.ser = ser;
   x.want_tail = false;
   x.tail_frac = -1.f;
   const EtdCfg ec{b.etd.modecutoff, b.etd.contour_radius, b.etd.contour_points};
@@ -1582,24 +1577,13 @@ RK_DEV void run_instance(const rk_batch& b, int inst, const Group& g, cx<T>* fa,
 }
 
 RK_HD constexpr size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
-static_assert(sizeof(k_ser_etd35) == sizeof(float) * 17 * RK_SER_NC * RK_SER_NT, "ETD35 series table size");
-static_assert(sizeof(k_ser_etd34) == sizeof(float) * 8 * RK_SER_NC * RK_SER_NT, "ETD34 series table size");
-// floats of the FP32 coefficient series table a method's rebuilds read (0: none)
-template <class T, int METHOD>
-RK_HD constexpr int ser_table_floats() {
-  return sizeof(T) != sizeof(float) ? 0
-         : (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? 17 * RK_SER_NC * RK_SER_NT
-         : (METHOD == RK_ETD34 || METHOD == RK_ETD4) ? 8 * RK_SER_NC * RK_SER_NT : 0;
-}
-// offset of the block-wide copies (learned-controller launches) and their bytes
+// offset of the block-wide copy of the inference buffer (learned-controller launches) and
+// its bytes
 template <class T, int LOGN>
 RK_HD constexpr size_t block_extra_offset(int ngroups, int group_smem) {
   return (size_t)ngroups * group_smem + (LOGN > 0 ? align16(sizeof(cx<T>) * twiddle_rows<LOGN>()) : 0);
 }
-template <class T, int METHOD>
-RK_HD constexpr size_t learned_extra_bytes() {
-  return align16(RK_MLP_PACK_BYTES) + align16(sizeof(float) * ser_table_floats<T, METHOD>());
-}
+RK_HD constexpr size_t learned_extra_bytes() { return align16(RK_MLP_PACK_BYTES); }
 
 // A block holds blockDim.x / gthreads independent groups; each group owns one slice of
 // shared memory: [fa | fb] FFT buffers of fpad_size(nfft) points, 64 doubles of reduction
@@ -1620,25 +1604,18 @@ __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const 
     fill_twiddle_rows<T, LOGN>(tws, reinterpret_cast<const cx<T>*>(b.twiddle), threadIdx.x, blockDim.x);
     __syncthreads();
   }
-  // Launches with the learned controller: the inference buffer and (FP32 ETD methods) the
-  // coefficient series table, copied once per block into shared memory after the group
-  // slices and the twiddle rows.  From global memory, the inference's weight reads and the
-  // every-attempt rebuilds' table reads missed the small L1 beside the shared memory.
+  // Launches with the learned controller: the inference buffer, copied once per block into
+  // shared memory after the group slices and the twiddle rows.  (The coefficient rebuilds,
+  // one per attempt under this controller, read the series table from global memory: a
+  // shared-memory copy reached through the out-of-line rebuild's pointer argument made each
+  // rebuild slower, 12 of 50 ms on 1546 Burgers instances to t = 5.)
   const unsigned char* mlpw = reinterpret_cast<const unsigned char*>(b.mlp);
-  const float* ser = nullptr;
   if (b.mlp != nullptr) {
     unsigned char* ex = smem + block_extra_offset<T, LOGN>(ngroups, group_smem);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(b.mlp);
     uint32_t* dst = reinterpret_cast<uint32_t*>(ex);
     for (int i = threadIdx.x; i < RK_MLP_PACK_BYTES / 4; i += blockDim.x) dst[i] = src[i];
     mlpw = ex;
-    constexpr int nser = ser_table_floats<T, METHOD>();
-    if constexpr (nser > 0) {
-      float* sr = reinterpret_cast<float*>(ex + align16(RK_MLP_PACK_BYTES));
-      const float* st = (METHOD == RK_ETD35 || METHOD == RK_ETD5) ? k_ser_etd35 : k_ser_etd34;
-      for (int i = threadIdx.x; i < nser; i += blockDim.x) sr[i] = st[i];
-      ser = sr;
-    }
     __syncthreads();
   }
   unsigned char* base = smem + (size_t)gi * group_smem;
@@ -1656,7 +1633,7 @@ __global__ void __launch_bounds__(512, 1) evolve_kernel(const rk_batch b, const 
     g.sync();
     if (item >= count) break;
     const int inst = order ? order[item] : item;
-    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s, nfft, mlpw, ser);
+    run_instance<T, CT, S, METHOD, LOGN, PLACE>(b, inst, g, fa, fb, red, sm_slab, tws, mlp_s, nfft, mlpw);
   }
 }
 

@@ -13,7 +13,7 @@ static int launch_evolve_v(const rk_batch& b, const ClassLaunch& c, cudaStream_t
   const int64_t m = (b.nl_kind == RK_NL_UUX) ? nfft / 2 + 1 : nfft;
   const size_t group_smem = (evolve_smem<T>(nfft) + smem_slab_bytes<T, CT, M>(PLACE, m) + 15) & ~size_t(15);
   const size_t sm = block_extra_offset<T, LOGN>(c.groups, (int)group_smem) +
-                   (b.mlp != nullptr ? learned_extra_bytes<T, M>() : 0);
+                   (b.mlp != nullptr ? learned_extra_bytes() : 0);
   const int block = c.threads * c.groups;
   auto kern = evolve_kernel<T, CT, S, M, LOGN, PLACE>;
   if (int e = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
