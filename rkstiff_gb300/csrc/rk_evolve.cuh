@@ -496,6 +496,30 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
   return cx<double>{h * L.x, h * L.y};
 }
 
+// FP32 ETD35 / ETD5 coefficients of one real mode into the block.  With the double-float
+// state (elo set) only e^(z/4) of the four exponentials is stored: the stage code forms
+// e^(z/2) = e14 e14, e^(3z/4) = e^(z/2) e14 and e^z = e^(z/2) e^(z/2) by rounded FP32
+// products (exp_pow), and the low word of e^z is taken against that product (e_hi + e_lo
+// = e^z as the rebuild formed it, e_hi = of[C35_E]), so the new state keeps its accuracy.
+// Three fewer arrays per instance pass through the stage loops and the L2.
+template <int METHOD>
+RK_DEV void put_coeffs_f32(float* __restrict__ C, int mp, int j, const float* of, float* __restrict__ elo,
+                           float e_lo) {
+  constexpr int NC = Traits<METHOD>::NC;
+  if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) {
+    if (elo) {
+      const float e12 = __fmul_rn(of[C35_E14], of[C35_E14]);
+      elo[j] = (of[C35_E] - __fmul_rn(e12, e12)) + e_lo;
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c != C35_E12 && c != C35_E34 && c != C35_E) C[c * mp + j] = of[c];
+      return;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+}
+
 // Coefficients of one instance at step h into C (array c at C + c*mp).  S is double for
 // a real operator (CT real) and cx<double> for a complex one.  FAST selects the
 // reduced-cost psi evaluation for real modes (coefficients stored in FP32).  Kept out of
@@ -531,10 +555,9 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
         if constexpr (sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float)) {
           // each combination's own Taylor series in FP32 (series_coeffs_f32): the FP64
           // series would hold the whole warp on the 1/64-rate FP64 pipe for one small mode
-          float of[NC];
-          series_coeffs_f32<METHOD>(sre(z), h, of, nullptr, elo ? elo + j : nullptr);
-#pragma unroll
-          for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+          float of[NC], el = 0.f;
+          series_coeffs_f32<METHOD>(sre(z), h, of, nullptr, &el);
+          put_coeffs_f32<METHOD>(C, mp, j, of, elo, el);
         } else {
           S E[4];
           taylor_psi<S>(METHOD, z, h, E, P);
@@ -553,28 +576,27 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
         // stiff: FP32 arithmetic in a form without cancellation (a few FP32 ulps)
         float of[NC];
         stiff_coeffs_f32<METHOD>(zr, h, of);
-        if (elo) elo[j] = 0.f;  // e^z < e^-32: its low word is below every other term
-#pragma unroll
-        for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+        put_coeffs_f32<METHOD>(C, mp, j, of, elo, 0.f);  // e^z < e^-32: no low word of its own
         continue;
       }
       if (zr <= 80.0) {
         // FP32 series / stiff forms per combination (series_coeffs_f32)
-        float of[NC];
-        series_coeffs_f32<METHOD>(zr, h, of, nullptr, elo ? elo + j : nullptr);
-#pragma unroll
-        for (int c = 0; c < NC; ++c) C[c * mp + j] = of[c];
+        float of[NC], el = 0.f;
+        series_coeffs_f32<METHOD>(zr, h, of, nullptr, &el);
+        put_coeffs_f32<METHOD>(C, mp, j, of, elo, el);
         continue;
       }
       double E[4];
       fast_real_psi(METHOD, zr, h, E, reinterpret_cast<double*>(P));
       etd_from_psi_e<double>(METHOD, E, reinterpret_cast<double*>(P), reinterpret_cast<double*>(o));
-      if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) {
-        if (elo) {
-          const double e = reinterpret_cast<double*>(o)[C35_E];
-          elo[j] = (float)(e - (double)(float)e);
-        }
-      }
+      const double* od = reinterpret_cast<const double*>(o);
+      float of[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) of[c] = (float)od[c];
+      float el = 0.f;
+      if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5) el = (float)(od[C35_E] - (double)of[C35_E]);
+      put_coeffs_f32<METHOD>(C, mp, j, of, elo, el);
+      continue;
     } else if constexpr (FAST && sizeof(S) == sizeof(double)) {
       double E[4];
       fast_real_psi(METHOD, sre(z), h, E, reinterpret_cast<double*>(P));
@@ -853,26 +875,50 @@ template <class T, class CT, int LOGN>
 RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, const rk_controller& ctl, int& nl_count) {
   const cx<T>* u = x.u;
   cx<T>* const* N = x.N;
+  // e^(z/2), e^(3z/4), e^z: FP32 with a real operator (the double-float state) keeps only
+  // e^(z/4) in the block and forms the others by the rounded products the rebuild took the
+  // low word of e^z against (put_coeffs_f32); otherwise loaded
+  constexpr bool EPOW = SlabShape<T, CT, RK_ETD35>::DF && sizeof(CT) == sizeof(float);
+  auto e12 = [&](int j) -> CT {
+    if constexpr (EPOW) return __fmul_rn(x.c(C35_E14, j), x.c(C35_E14, j));
+    else return x.c(C35_E12, j);
+  };
+  auto e34 = [&](int j) -> CT {
+    if constexpr (EPOW) {
+      const float a = x.c(C35_E14, j);
+      return __fmul_rn(__fmul_rn(a, a), a);
+    } else {
+      return x.c(C35_E34, j);
+    }
+  };
+  auto e1 = [&](int j) -> CT {
+    if constexpr (EPOW) {
+      const float a = x.c(C35_E14, j), b = __fmul_rn(a, a);
+      return __fmul_rn(b, b);
+    } else {
+      return x.c(C35_E, j);
+    }
+  };
   // rkstiff/etd35.py:320-345 (ETD5: etd5.py:236-260)
   nl_eval(x, [&](int j) { return cmul(x.c(C35_E14, j), u[j]) + cmul(x.c(C35_A21, j), N[0][j]); }, N[1]);
   nl_eval(x, [&](int j) {
     return (cmul(x.c(C35_E14, j), u[j]) + cmul(x.c(C35_A31, j), N[0][j])) + cmul(x.c(C35_A32, j), N[1][j]);
   }, N[2]);
   nl_eval(x, [&](int j) {
-    return (cmul(x.c(C35_E12, j), u[j]) + cmul(x.c(C35_A41, j), N[0][j])) + cmul(x.c(C35_A43, j), N[2][j]);
+    return (cmul(e12(j), u[j]) + cmul(x.c(C35_A41, j), N[0][j])) + cmul(x.c(C35_A43, j), N[2][j]);
   }, N[3]);
   nl_eval(x, [&](int j) {
-    return ((cmul(x.c(C35_E34, j), u[j]) + cmul(x.c(C35_A51, j), N[0][j])) + cmul(x.c(C35_A52, j), N[1][j] - N[2][j])) +
+    return ((cmul(e34(j), u[j]) + cmul(x.c(C35_A51, j), N[0][j])) + cmul(x.c(C35_A52, j), N[1][j] - N[2][j])) +
            cmul(x.c(C35_A54, j), N[3][j]);
   }, N[4]);
   nl_eval(x, [&](int j) {
     cx<T> t = N[1][j] - (T(3) * N[3][j]) * T(0.5);
-    return (((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A61, j), N[0][j])) + cmul(x.c(C35_A62, j), t)) +
+    return (((cmul(e1(j), u[j]) + cmul(x.c(C35_A61, j), N[0][j])) + cmul(x.c(C35_A62, j), t)) +
             cmul(x.c(C35_A63, j), N[2][j])) + cmul(x.c(C35_A65, j), N[4][j]);
   }, N[5]);
   nl_count += 5;
   auto k7 = [&](int j) {
-    return ((((cmul(x.c(C35_E, j), u[j]) + cmul(x.c(C35_A71, j), N[0][j])) + cmul(x.c(C35_A73, j), N[2][j])) +
+    return ((((cmul(e1(j), u[j]) + cmul(x.c(C35_A71, j), N[0][j])) + cmul(x.c(C35_A73, j), N[2][j])) +
              cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) + cmul(x.c(C35_A76, j), N[5][j]);
   };
   // Double-float state (x.ulo set: FP32): unew = E u + S with u = u_hi +
@@ -886,7 +932,7 @@ RK_DEV double attempt_etd35_family(const Ctx<T, CT, LOGN>& x, bool adaptive, con
       const cx<T> S = (((cmul(x.c(C35_A71, j), N[0][j]) + cmul(x.c(C35_A73, j), N[2][j])) +
                         cmul(x.c(C35_A74, j), N[3][j])) + cmul(x.c(C35_A75, j), N[4][j])) +
                       cmul(x.c(C35_A76, j), N[5][j]);
-      const float eh = x.c(C35_E, j), el = x.c(C35_N, j);
+      const float eh = e1(j), el = x.c(C35_N, j);
       const cx<T> uh = u[j], ul = x.ulo[j];
       auto part = [&](float h, float l, float sv, float& lo_out) {
         const float p = eh * h;
