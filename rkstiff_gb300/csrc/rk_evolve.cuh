@@ -156,8 +156,8 @@ struct Ctx {
 // Hermitian spectra of u and u_x: Z[j] = (A.x - B.y, A.y + B.x) and Z[n-j] = (A.x + B.y, B.x -
 // A.y) for 0 < j < n/2, the imaginary parts of A and B dropped at j = 0 and n/2 (as numpy's
 // irfft drops them).  Butterfly c of the pass needs Z[c + r NB0], r < R0: the rows r < R0/2
-// are modes of column c, the others mirror images of the modes of column NB0 - c.  A lane
-// pair holds the columns c and NB0 - c (paired_column), so each lane evaluates kf for the
+// are modes of column c, the others mirror images of the modes of column NB0 - c.  Two
+// partner lanes hold the columns c and NB0 - c (paired_column), so each lane evaluates kf for the
 // R0/2 modes of its own column and swaps the mirror images with its partner by shuffles;
 // columns 0 and NB0/2 mirror themselves (column 0 also takes the Nyquist mode n/2).  Every
 // mode is evaluated once, and the packed spectrum never goes through shared memory.
@@ -180,7 +180,7 @@ RK_DEV void pack_first_pass(const Group& g, KF kf, const T* __restrict__ kx, cx<
   };
   for (int tt = g.tid; tt < NB0; tt += g.nthr) {
     const int c = paired_column(tt, NB0);
-    const bool self = (tt >> 1) == 0;  // columns 0 and NB0/2: their own mirror images
+    const bool self = pair_unit(tt) == 0;  // columns 0 and NB0/2: their own mirror images
     const bool col0 = c == 0;
     cx<T> v[R0], mir[H], nyq{T(0), T(0)}, unused;
 #pragma unroll
@@ -206,7 +206,7 @@ RK_DEV void pack_first_pass(const Group& g, KF kf, const T* __restrict__ kx, cx<
 // Last pass of the forward n/2-point transform fused with the rfft split.  Butterfly k (k <
 // NB, the pass's sub-length) produces F[k + r NB], r < Rf; rfft mode k' = k + r NB needs F[k']
 // and conj(F[n/2 - k']), and n/2 - k' = (NB - k) + (Rf - 1 - r) NB is an output of butterfly
-// NB - k: with the butterflies paired over lane pairs (paired_column) the partner's outputs
+// NB - k: with the butterflies paired over partner lanes (paired_column) the partner's outputs
 // arrive by shuffles, and each lane writes the Rf modes of its butterfly (butterfly 0 also
 // the Nyquist mode n/2) with no pass through shared memory.
 // mode k': out = ((F + conj(Fm))/2 + W_n^k' (-i)(F - conj(Fm))/2) c.  W_n^k': FP32 from row 1
@@ -236,7 +236,7 @@ RK_DEV void fwd_last_split(const Group& g, const cx<T>* __restrict__ x, const cx
   };
   for (int tt = g.tid; tt < NB; tt += g.nthr) {
     const int k = paired_column(tt, NB);
-    const bool self = (tt >> 1) == 0;
+    const bool self = pair_unit(tt) == 0;
     const bool col0 = k == 0;
     const cx<T>* xi = x + fpad(k);
     cx<T> v[Rf];
@@ -611,10 +611,13 @@ __device__ __noinline__ void compute_coeffs_impl(Group g, int m, int mp, const c
       }
       etd_from_psi<S>(METHOD, z, P, o);
     }
+    // (the FP32 real-operator branch above stores its modes itself)
+    if constexpr (!(FAST && sizeof(S) == sizeof(double) && sizeof(CT) == sizeof(float))) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
-    if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5)
-      if (elo) store_lo(elo[j], o[C35_E]);
+      for (int c = 0; c < NC; ++c) store_c(C[c * mp + j], o[c]);
+      if constexpr (METHOD == RK_ETD35 || METHOD == RK_ETD5)
+        if (elo) store_lo(elo[j], o[C35_E]);
+    }
   }
   if constexpr (FAST) {
     g.sync();
