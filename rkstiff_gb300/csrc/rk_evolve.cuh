@@ -157,10 +157,11 @@ struct Ctx {
 // A.y) for 0 < j < n/2, the imaginary parts of A and B dropped at j = 0 and n/2 (as numpy's
 // irfft drops them).  Butterfly c of the pass needs Z[c + r NB0], r < R0: the rows r < R0/2
 // are modes of column c, the others mirror images of the modes of column NB0 - c.  Two
-// partner lanes hold the columns c and NB0 - c (paired_column), so each lane evaluates kf for the
-// R0/2 modes of its own column and swaps the mirror images with its partner by shuffles;
-// columns 0 and NB0/2 mirror themselves (column 0 also takes the Nyquist mode n/2).  Every
-// mode is evaluated once, and the packed spectrum never goes through shared memory.
+// partner lanes hold the columns c and NB0 - c (paired_column), so each lane evaluates kf
+// for the R0/2 modes of its own column and swaps the mirror images with its partner by
+// shuffles; columns 0 and NB0/2 mirror themselves (column 0 also takes the Nyquist mode
+// n/2).  Every mode is evaluated once, and the packed spectrum never goes through shared
+// memory.
 template <class T, int LOGN, class KF>
 RK_DEV void pack_first_pass(const Group& g, KF kf, const T* __restrict__ kx, cx<T>* __restrict__ y, T inv_n) {
   using P0 = PassInfo<LOGN, 0>;
@@ -499,9 +500,10 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
 // FP32 ETD35 / ETD5 coefficients of one real mode into the block.  With the double-float
 // state (elo set) only e^(z/4) of the four exponentials is stored: the stage code forms
 // e^(z/2) = e14 e14, e^(3z/4) = e^(z/2) e14 and e^z = e^(z/2) e^(z/2) by rounded FP32
-// products (exp_pow), and the low word of e^z is taken against that product (e_hi + e_lo
-// = e^z as the rebuild formed it, e_hi = of[C35_E]), so the new state keeps its accuracy.
-// Three fewer arrays per instance pass through the stage loops and the L2.
+// products (e12 / e34 / e1 in attempt_etd35_family), and the low word of e^z is taken against
+// that product (e_hi + e_lo
+// = e^z as the rebuild formed it, e_hi = of[C35_E]), so the new state keeps its
+// accuracy.  Three fewer arrays per instance pass through the stage loops and the L2.
 template <int METHOD>
 RK_DEV void put_coeffs_f32(float* __restrict__ C, int mp, int j, const float* of, float* __restrict__ elo,
                            float e_lo) {
