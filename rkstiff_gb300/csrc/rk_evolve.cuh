@@ -500,10 +500,10 @@ template <> RK_DEV cx<double> load_z<cx<double>>(const cx<double>* lin, int j, d
 // FP32 ETD35 / ETD5 coefficients of one real mode into the block.  With the double-float
 // state (elo set) only e^(z/4) of the four exponentials is stored: the stage code forms
 // e^(z/2) = e14 e14, e^(3z/4) = e^(z/2) e14 and e^z = e^(z/2) e^(z/2) by rounded FP32
-// products (e12 / e34 / e1 in attempt_etd35_family), and the low word of e^z is taken against
-// that product (e_hi + e_lo
-// = e^z as the rebuild formed it, e_hi = of[C35_E]), so the new state keeps its
-// accuracy.  Three fewer arrays per instance pass through the stage loops and the L2.
+// products (e12 / e34 / e1 in attempt_etd35_family), and the low word of e^z is taken
+// against that product (e_hi + e_lo = e^z as the rebuild formed it, e_hi = of[C35_E]), so
+// the new state keeps its accuracy.  Three fewer arrays per instance pass through the stage
+// loops and the L2.
 template <int METHOD>
 RK_DEV void put_coeffs_f32(float* __restrict__ C, int mp, int j, const float* of, float* __restrict__ elo,
                            float e_lo) {
